@@ -1,0 +1,171 @@
+/*
+ * gbwt.h -- C ABI of the GB300 prefix-free-parsing (PFP) BWT library.
+ *
+ * The reference project is a set of stand-alone CUDA programs whose only
+ * interface is `main()` reading ./input.txt and writing ./out.txt, with the
+ * trigger parameters W and P fixed per binary by #define
+ * (Prefix_Free_Parsing_W=5_P=16_kommentiert.cu, "K" below, K:16-23 and
+ * Makefile:11-23).  Its internal API is a set of void functions over global
+ * device pointers (K:36-98).  This header replaces that surface with plain
+ * C entry points; the storage/return-code style follows the one real
+ * library API inside the reference, libcubwt (libcubwt.cuh:32-101).
+ *
+ * Conventions shared by every entry point:
+ *  - Return values >= 0 mean success; negative values are GBWT_* error
+ *    codes.  No entry point traps or asserts on the device: where the
+ *    reference asserts (K:130-132 input range, K:584-585 phrase length) this
+ *    library returns an error code or handles the case.
+ *  - Text bytes must lie in [2,254] (K:130-132); byte 1 is the implicit
+ *    sentinel, W copies of which are appended internally (K:146-149).
+ *    With GBWT_FLAG_SMALL_ALPHABET the bytes must lie in [2,15], the range
+ *    in which the reference's two-symbols-per-digit packing is exact
+ *    (Prefix_Free_Parsing_W=5_P=16_small_alphabet.cu:995-1002).
+ *  - The output has exactly n bytes in the reference's convention
+ *    (K:3325-3326, K:4776-4790): row i is the byte preceding the i-th
+ *    smallest suffix of T, with T[n-1] preceding the whole text.
+ *  - All device work runs on the storage's CUDA stream; calls on one
+ *    storage object must not overlap.  One storage object per host thread.
+ */
+#ifndef GBWT_H
+#define GBWT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBWT_VERSION_MAJOR 1
+#define GBWT_VERSION_MINOR 0
+
+/* Error codes; the first five keep libcubwt's values (libcubwt.cuh:32-38). */
+#define GBWT_NO_ERROR              0
+#define GBWT_BAD_PARAMETER        (-1)
+#define GBWT_NOT_ENOUGH_MEMORY    (-2)
+#define GBWT_GPU_ERROR            (-7)
+#define GBWT_GPU_NOT_SUPPORTED    (-8)
+#define GBWT_GPU_NOT_ENOUGH_MEMORY (-9)
+#define GBWT_UNSUPPORTED_INPUT    (-5)   /* outside the variant's domain     */
+#define GBWT_TIMEOUT              (-6)   /* a bounded device wait ran out    */
+#define GBWT_INTERNAL_ERROR       (-10)
+
+/* Flags. */
+#define GBWT_FLAG_SMALL_ALPHABET  1u  /* the *_small_alphabet.cu variants   */
+#define GBWT_FLAG_DEVICE_POINTERS 2u  /* T and L are device pointers        */
+#define GBWT_FLAG_STAGE_TIMES     4u  /* record per-stage CUDA-event times  */
+
+/* Counts of the last pipeline run on a storage object. */
+typedef struct gbwt_stats {
+    int64_t n;              /* text length                                   */
+    int64_t z;              /* phrase occurrences (K: size_D)                */
+    int64_t d;              /* distinct phrases                              */
+    int64_t dict_bytes;     /* sum of distinct phrase lengths                */
+    int64_t s;              /* |S|: distinct phrase suffixes longer than W   */
+    int64_t s_elems;        /* (phrase, offset) pairs behind S               */
+    int64_t mixed_blocks;   /* S entries whose BWT block is not one run      */
+    int64_t mixed_elems;    /* BWT bytes inside mixed blocks                 */
+    int64_t dict_rounds;    /* prefix-doubling rounds, dictionary sort       */
+    int64_t parse_rounds;   /* prefix-doubling rounds, parse suffix array    */
+    int64_t hash_retries;   /* fingerprint retries (collision or table full)  */
+    int64_t kernel_launches;/* kernels launched by the last call             */
+    int64_t primary_index;  /* output row of the suffix starting at T[0]
+                               (libcubwt's primary index minus one)          */
+    int64_t probe_launches; /* launches of the probed kernel (see below)     */
+    int64_t probe_bytes;    /* their algorithmic bytes                       */
+    double  probe_ms;       /* their summed CUDA-event durations             */
+    float   stage_ms[8];    /* with GBWT_FLAG_STAGE_TIMES: scan, phrases,
+                               dictionary, parse SA, S groups, runs, mixed,
+                               total                                          */
+} gbwt_stats;
+
+/*
+ * Allocates a storage object (stream, scratch pools) for texts of up to
+ * max_length bytes on the current CUDA device.  Replaces
+ * Malloc_And_Copy_On_GPU (K:175-188) and mirrors
+ * libcubwt_allocate_device_storage (libcubwt.cuh:48-57).  Scratch grows on
+ * first use and is reused afterwards, so repeated calls of the same size do
+ * not allocate.
+ */
+int64_t gbwt_allocate_device_storage(void **storage, int64_t max_length);
+
+/* Frees a storage object (libcubwt.cuh:59). */
+int64_t gbwt_free_device_storage(void *storage);
+
+/*
+ * Makes the storage issue its work on `cuda_stream` (a cudaStream_t, NULL =
+ * the storage's own stream).  No counterpart in the reference, which uses
+ * the default stream only; needed to time the pipeline on a caller stream.
+ */
+int64_t gbwt_set_stream(void *storage, void *cuda_stream);
+
+/*
+ * PFP BWT of one text: T[0..n) -> L[0..n).  Replaces the process-level
+ * pipeline of the reference's main() (K:4793-4815: Compute_D K:2415-2506,
+ * then Compute_S K:4330-4771) for one (W, P, small_alphabet) variant
+ * (Makefile:11-23).  W in [1,64], P in [2,65535].  Returns n on success.
+ */
+int64_t gbwt_pfp_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n,
+                     int32_t W, int32_t P, uint32_t flags);
+
+/*
+ * Trigger scan only: writes the phrase end positions D[0..z) (the last is
+ * n+W-1) and returns z.  Replaces Compute_D1/D2/D3 (K:443-576, driver
+ * K:2415-2455).  Returns GBWT_BAD_PARAMETER when capacity < z.
+ */
+int64_t gbwt_pfp_trigger_scan(void *storage, const uint8_t *T, int64_t n, int32_t W,
+                              int32_t P, uint32_t flags, int64_t *D, int64_t capacity);
+
+/*
+ * Parse of the text: for every phrase occurrence k, the dense lexicographic
+ * rank of its phrase among the distinct phrases (ranks[0..z)), and the
+ * suffix array of that parse (parse_sa[0..z), may be NULL).  Replaces the
+ * phrase sort + meta-characters + parse suffix array of the reference
+ * (K:1990-2164, K:616-691, K:2342-2412); the reference's meta-character is
+ * the sorted index of the last occurrence of an equal phrase, which orders
+ * phrases exactly like the dense rank returned here.  Returns z.
+ */
+int64_t gbwt_pfp_parse(void *storage, const uint8_t *T, int64_t n, int32_t W, int32_t P,
+                       uint32_t flags, int32_t *ranks, int32_t *parse_sa, int64_t capacity);
+
+/* Copies the counts of the last call into *out. */
+int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
+
+/* Kernels that can be probed (timed launch by launch with CUDA events). */
+#define GBWT_PROBE_NONE           (-1)
+#define GBWT_PROBE_RADIX_SCATTER    1   /* radix-sort scatter pass          */
+#define GBWT_PROBE_TRIGGER_SCAN     2   /* trigger scan (count and write)   */
+#define GBWT_PROBE_PHRASE_HASH      3   /* phrase fingerprint + table insert */
+#define GBWT_PROBE_RUN_FILL         4   /* run blocks written to the output */
+#define GBWT_PROBE_MIXED_SCATTER    5   /* mixed-block bytes scattered      */
+
+/*
+ * Starts timing every launch of one kernel family (GBWT_PROBE_*) on the
+ * storage's stream, accumulating launches, algorithmic bytes and event time
+ * into the probe_* fields of gbwt_stats across calls until the next
+ * gbwt_set_kernel_probe.  No counterpart in the reference (it was profiled
+ * externally with nsys, Benchmark_Skript_Linux.sh:85).
+ */
+int64_t gbwt_set_kernel_probe(void *storage, int32_t kernel);
+
+/*
+ * Reads the reference's input format (K:111-150, Scan_input): a decimal
+ * count n, then n whitespace-separated decimal byte values.  *T is
+ * malloc'ed (release with gbwt_free_host); returns n.  Values outside
+ * [2,254] give GBWT_BAD_PARAMETER, where the reference asserts.
+ */
+int64_t gbwt_read_input_txt(const char *path, uint8_t **T, int64_t *n);
+
+/* Writes the reference's output format (K:4776-4790, print_Output). */
+int64_t gbwt_write_out_txt(const char *path, const uint8_t *L, int64_t n);
+
+/* Releases memory returned by gbwt_read_input_txt. */
+void gbwt_free_host(void *p);
+
+/* Static description of an error code. */
+const char *gbwt_error_string(int64_t code);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBWT_H */

@@ -1,0 +1,293 @@
+"""GB300-native prefix-free-parsing (PFP) BWT construction.
+
+Python host interface over the C ABI of ``libgbwt.so`` (include/gbwt.h).  It
+mirrors the reference programs' surface: a text of bytes in [2,254], the
+trigger parameters W and P (plus the small-alphabet variants), and the BWT
+byte array in the reference's convention (Prefix_Free_Parsing_W=5_P=16
+_kommentiert.cu, "K": Scan_input K:111-150, Compute_D K:2415-2506,
+Compute_S K:4330-4771, print_Output K:4776-4790).
+
+There is no CPU fallback: without the built CUDA library every compute call
+raises ``GbwtLibraryMissing``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbwt.so")
+
+# Error codes (include/gbwt.h).
+NO_ERROR = 0
+BAD_PARAMETER = -1
+NOT_ENOUGH_MEMORY = -2
+UNSUPPORTED_INPUT = -5
+TIMEOUT = -6
+GPU_ERROR = -7
+GPU_NOT_SUPPORTED = -8
+GPU_NOT_ENOUGH_MEMORY = -9
+INTERNAL_ERROR = -10
+
+FLAG_SMALL_ALPHABET = 1
+FLAG_DEVICE_POINTERS = 2
+FLAG_STAGE_TIMES = 4
+
+# The reference's binaries (Makefile:11-23) and their (W, P, small) variants.
+VARIANTS = {
+    "Prefix_Free_Parsing_W=5_P=16": (5, 16, False),
+    "Prefix_Free_Parsing_W=5_P=14": (5, 14, False),
+    "Prefix_Free_Parsing_W=5_P=13": (5, 13, False),
+    "Prefix_Free_Parsing_W=5_P=11": (5, 11, False),
+    "Prefix_Free_Parsing_W=5_P=23": (5, 23, False),
+    "Prefix_Free_Parsing_W=35_P=81_small_alphabet": (35, 81, True),
+    "Prefix_Free_Parsing_W=5_P=16_small_alphabet": (5, 16, True),
+    "Prefix_Free_Parsing_W=5_P=23_small_alphabet": (5, 23, True),
+    "Prefix_Free_Parsing_W=5_P=14_small_alphabet": (5, 14, True),
+}
+
+STAGES = ("scan", "phrases", "dictionary", "parse_sa", "s_groups", "runs", "mixed", "total")
+
+
+class GbwtError(RuntimeError):
+    """A negative return code of the C ABI."""
+
+    def __init__(self, code: int, where: str = ""):
+        self.code = int(code)
+        msg = _lib().gbwt_error_string(self.code).decode() if _LIB is not None else str(code)
+        super().__init__(f"{where}: {msg} ({self.code})" if where else f"{msg} ({self.code})")
+
+
+class GbwtLibraryMissing(ImportError):
+    pass
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in (
+        "n", "z", "d", "dict_bytes", "s", "s_elems", "mixed_blocks", "mixed_elems",
+        "dict_rounds", "parse_rounds", "hash_retries", "kernel_launches", "primary_index",
+        "probe_launches", "probe_bytes")] + [("probe_ms", ctypes.c_double), ("stage_ms", ctypes.c_float * 8)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}
+        d["stage_ms"] = {name: float(self.stage_ms[i]) for i, name in enumerate(STAGES)}
+        return d
+
+
+_LIB = None
+
+# Every exported entry point of include/gbwt.h.
+EXPORTS = (
+    "gbwt_allocate_device_storage", "gbwt_free_device_storage", "gbwt_set_stream", "gbwt_pfp_bwt",
+    "gbwt_pfp_trigger_scan", "gbwt_pfp_parse", "gbwt_get_stats", "gbwt_read_input_txt",
+    "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
+)
+
+PROBE_NONE = -1
+PROBE_RADIX_SCATTER = 1
+PROBE_TRIGGER_SCAN = 2
+PROBE_PHRASE_HASH = 3
+PROBE_RUN_FILL = 4
+PROBE_MIXED_SCATTER = 5
+
+
+def _lib() -> ctypes.CDLL:
+    """Loads libgbwt.so (built by build.py); raises if it is missing."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise GbwtLibraryMissing(
+            f"{LIB_PATH} is not built; run __graft_entry__.build() (no CPU fallback exists)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u8p, i64, i32, u32 = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_uint32
+    L.gbwt_allocate_device_storage.argtypes = [ctypes.POINTER(vp), i64]
+    L.gbwt_allocate_device_storage.restype = i64
+    L.gbwt_free_device_storage.argtypes = [vp]
+    L.gbwt_free_device_storage.restype = i64
+    L.gbwt_set_stream.argtypes = [vp, vp]
+    L.gbwt_set_stream.restype = i64
+    L.gbwt_pfp_bwt.argtypes = [vp, u8p, u8p, i64, i32, i32, u32]
+    L.gbwt_pfp_bwt.restype = i64
+    L.gbwt_pfp_trigger_scan.argtypes = [vp, u8p, i64, i32, i32, u32, ctypes.c_void_p, i64]
+    L.gbwt_pfp_trigger_scan.restype = i64
+    L.gbwt_pfp_parse.argtypes = [vp, u8p, i64, i32, i32, u32, ctypes.c_void_p, ctypes.c_void_p, i64]
+    L.gbwt_pfp_parse.restype = i64
+    L.gbwt_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.gbwt_get_stats.restype = i64
+    L.gbwt_read_input_txt.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(i64)]
+    L.gbwt_read_input_txt.restype = i64
+    L.gbwt_write_out_txt.argtypes = [ctypes.c_char_p, u8p, i64]
+    L.gbwt_write_out_txt.restype = i64
+    L.gbwt_free_host.argtypes = [vp]
+    L.gbwt_free_host.restype = None
+    L.gbwt_error_string.argtypes = [i64]
+    L.gbwt_error_string.restype = ctypes.c_char_p
+    L.gbwt_set_kernel_probe.argtypes = [vp, i32]
+    L.gbwt_set_kernel_probe.restype = i64
+    _LIB = L
+    return L
+
+
+def _check(rc: int, where: str) -> int:
+    if rc < 0:
+        raise GbwtError(rc, where)
+    return rc
+
+
+def _host_u8(a) -> np.ndarray:
+    if isinstance(a, (bytes, bytearray, memoryview)):
+        a = np.frombuffer(bytes(a), dtype=np.uint8)
+    return np.ascontiguousarray(a, dtype=np.uint8)
+
+
+class Storage:
+    """Device storage (stream + scratch pools), libcubwt_allocate_device_storage
+    style (libcubwt.cuh:48-59).  Use one per thread; reuse across calls."""
+
+    def __init__(self, max_length: int = 0):
+        self._p = ctypes.c_void_p()
+        _check(_lib().gbwt_allocate_device_storage(ctypes.byref(self._p), int(max_length)),
+               "gbwt_allocate_device_storage")
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if not self._p:
+            raise ValueError("storage is closed")
+        return self._p
+
+    def close(self) -> None:
+        if self._p:
+            _lib().gbwt_free_device_storage(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        _check(_lib().gbwt_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)), "gbwt_set_stream")
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(_lib().gbwt_get_stats(self.handle, ctypes.byref(s)), "gbwt_get_stats")
+        return s.as_dict()
+
+    # -- compute ---------------------------------------------------------
+    def pfp_bwt(self, text, W: int = 5, P: int = 16, small_alphabet: bool = False,
+                stage_times: bool = False) -> np.ndarray:
+        t = _host_u8(text)
+        out = np.empty(max(len(t), 1), dtype=np.uint8)
+        flags = (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (FLAG_STAGE_TIMES if stage_times else 0)
+        _check(_lib().gbwt_pfp_bwt(self.handle, t.ctypes.data, out.ctypes.data, len(t), W, P, flags),
+               "gbwt_pfp_bwt")
+        return out[:len(t)]
+
+    def pfp_bwt_into(self, text: np.ndarray, out: np.ndarray, W: int = 5, P: int = 16,
+                     small_alphabet: bool = False) -> int:
+        """Host buffers owned by the caller (e.g. pinned): text -> out."""
+        if text.dtype != np.uint8 or out.dtype != np.uint8 or not text.flags.c_contiguous \
+                or not out.flags.c_contiguous or len(out) < len(text):
+            raise ValueError("text/out must be contiguous uint8 arrays, len(out) >= len(text)")
+        flags = FLAG_SMALL_ALPHABET if small_alphabet else 0
+        return _check(_lib().gbwt_pfp_bwt(self.handle, text.ctypes.data, out.ctypes.data, len(text), W, P, flags),
+                      "gbwt_pfp_bwt")
+
+    def set_kernel_probe(self, kernel: int) -> None:
+        """Time every launch of one kernel family (PROBE_*) from now on."""
+        _check(_lib().gbwt_set_kernel_probe(self.handle, int(kernel)), "gbwt_set_kernel_probe")
+
+    def pfp_bwt_device(self, text_ptr: int, out_ptr: int, n: int, W: int = 5, P: int = 16,
+                       small_alphabet: bool = False, stage_times: bool = False) -> int:
+        """Device-pointer variant: ``text_ptr``/``out_ptr`` are CUDA device addresses."""
+        flags = FLAG_DEVICE_POINTERS | (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (
+            FLAG_STAGE_TIMES if stage_times else 0)
+        return _check(_lib().gbwt_pfp_bwt(self.handle, ctypes.c_void_p(text_ptr), ctypes.c_void_p(out_ptr), n, W, P,
+                                          flags), "gbwt_pfp_bwt")
+
+    def trigger_scan(self, text, W: int = 5, P: int = 16, small_alphabet: bool = False) -> np.ndarray:
+        t = _host_u8(text)
+        if len(t) == 0:
+            return np.zeros(0, dtype=np.int64)
+        D = np.empty(len(t) + 2, dtype=np.int64)
+        z = _check(_lib().gbwt_pfp_trigger_scan(self.handle, t.ctypes.data, len(t), W, P,
+                                                FLAG_SMALL_ALPHABET if small_alphabet else 0, D.ctypes.data, len(D)),
+                   "gbwt_pfp_trigger_scan")
+        return D[:z].copy()
+
+    def parse(self, text, W: int = 5, P: int = 16, small_alphabet: bool = False):
+        """(dense lexicographic phrase rank per occurrence, suffix array of the parse)."""
+        t = _host_u8(text)
+        if len(t) == 0:
+            return np.zeros(0, dtype=np.int32), np.zeros(0, dtype=np.int32)
+        cap = len(t) + 2
+        ranks = np.empty(cap, dtype=np.int32)
+        psa = np.empty(cap, dtype=np.int32)
+        z = _check(_lib().gbwt_pfp_parse(self.handle, t.ctypes.data, len(t), W, P,
+                                         FLAG_SMALL_ALPHABET if small_alphabet else 0, ranks.ctypes.data,
+                                         psa.ctypes.data, cap), "gbwt_pfp_parse")
+        return ranks[:z].copy(), psa[:z].copy()
+
+
+_DEFAULT: Storage | None = None
+
+
+def default_storage() -> Storage:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Storage(0)
+    return _DEFAULT
+
+
+def pfp_bwt(text, W: int = 5, P: int = 16, small_alphabet: bool = False) -> np.ndarray:
+    """BWT of ``text`` (bytes in [2,254]) in the reference's output convention."""
+    return default_storage().pfp_bwt(text, W, P, small_alphabet)
+
+
+def variant(name: str) -> tuple[int, int, bool]:
+    """(W, P, small_alphabet) of a reference binary name (with or without _Linux)."""
+    base = os.path.basename(name)
+    if base.endswith("_Linux"):
+        base = base[: -len("_Linux")]
+    if base.endswith(".cu"):
+        base = base[:-3]
+    return VARIANTS[base]
+
+
+# -- reference file formats --------------------------------------------------
+def scan_input(path: str) -> np.ndarray:
+    """Reads the reference's input.txt (K:111-150)."""
+    L = _lib()
+    p = ctypes.c_void_p()
+    n = ctypes.c_int64()
+    rc = L.gbwt_read_input_txt(path.encode(), ctypes.byref(p), ctypes.byref(n))
+    _check(rc, "gbwt_read_input_txt")
+    try:
+        return np.ctypeslib.as_array((ctypes.c_uint8 * max(n.value, 1)).from_address(p.value))[: n.value].copy() \
+            if n.value else np.zeros(0, dtype=np.uint8)
+    finally:
+        L.gbwt_free_host(p)
+
+
+def print_output(path: str, L_bytes) -> None:
+    """Writes the reference's out.txt (K:4776-4790)."""
+    a = _host_u8(L_bytes)
+    _check(_lib().gbwt_write_out_txt(path.encode(), a.ctypes.data, len(a)), "gbwt_write_out_txt")
+
+
+@dataclass
+class Variant:
+    W: int
+    P: int
+    small_alphabet: bool = False

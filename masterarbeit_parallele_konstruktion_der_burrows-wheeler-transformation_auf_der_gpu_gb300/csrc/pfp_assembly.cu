@@ -1,0 +1,374 @@
+// pfp_assembly.cu -- BWT assembly from the dictionary order and the parse
+// suffix array (sm_103a).
+//
+// The reference enumerates S (distinct phrase suffixes longer than W) from a
+// colex sort of all occurrences, finds each entry's colex interval with a
+// next-smaller-value search, writes one-byte blocks ("runs") directly and
+// sorts the remaining ("mixed") blocks by the rank of the next parse suffix
+// (Prefix_Free_Parsing_W=5_P=16_kommentiert.cu, "K": Compute_S1..S6
+// K:2509-3369, bitonic block sorts K:3556-4248).
+//
+// Here S comes out of the dictionary suffix order directly: equal suffixes
+// are one group of the prefix-doubling result.  For every group we add the
+// occurrence counts of its phrases (block length) and check whether all
+// preceding bytes agree (run).  Runs are written tile by tile with 16-byte
+// stores.  For mixed groups, every phrase occurrence -- visited in parse
+// suffix-array order, which is exactly the "rank of the next parse suffix"
+// order the reference sorts by -- emits one (group, byte) element per mixed
+// suffix of its phrase; one stable radix sort by group then places every
+// byte, and a coalesced scatter writes them into the output.
+#include "prims.cuh"
+
+namespace gbwt {
+
+constexpr uint32_t PC_VAR = 0x100u;     // "byte preceding the occurrence"
+
+struct PosInfo {
+    const uint32_t *dphr, *doff, *dlen;
+    __device__ __forceinline__ void get(uint32_t x, uint32_t &q, uint32_t &off, uint32_t &rem) const
+    {
+        q = dphr[x];
+        off = x - doff[q];
+        rem = dlen[q] - off;
+    }
+};
+
+// Preceding-byte code of the phrase suffix starting at dictionary position x.
+__device__ __forceinline__ uint32_t pc_code(const uint8_t *dict, const uint32_t *pcmin, const uint32_t *pcmax,
+                                            uint32_t x, uint32_t q, uint32_t off)
+{
+    if (off) return dict[x - 1];
+    return pcmin[q] == pcmax[q] ? pcmin[q] : PC_VAR;
+}
+
+// Pass 1 over the dictionary order: S elements, group index, block lengths.
+struct LoadSHead {
+    const uint32_t *sa, *isa;
+    PosInfo pi;
+    uint32_t W;
+    __device__ __forceinline__ uint32_t operator()(size_t t) const
+    {
+        uint32_t x = sa[t], q, off, rem;
+        pi.get(x, q, off, rem);
+        return (rem > W && isa[x] == (uint32_t)t) ? 1u : 0u;
+    }
+};
+struct StoreSGroup {
+    const uint32_t *sa;
+    PosInfo pi;
+    uint32_t W;
+    const uint8_t *dict;
+    const uint32_t *occ, *pcmin, *pcmax;
+    uint32_t *gcount;
+    uint16_t *gchar;
+    uint32_t *grp_of;
+    __device__ __forceinline__ void operator()(size_t t, uint32_t inc, uint32_t v) const
+    {
+        uint32_t x = sa[t], q, off, rem;
+        pi.get(x, q, off, rem);
+        if (rem <= W) return;
+        const uint32_t g = inc - 1u;
+        grp_of[x] = g;
+        atomicAdd(gcount + g, occ[q]);
+        if (v) gchar[g] = (uint16_t)pc_code(dict, pcmin, pcmax, x, q, off);
+    }
+};
+
+// Pass 2 over dictionary positions: mark groups with differing bytes.
+__global__ void k_mark_mixed(uint32_t N, PosInfo pi, uint32_t W, const uint8_t *dict, const uint32_t *pcmin,
+                             const uint32_t *pcmax, const uint32_t *grp_of, const uint16_t *gchar, uint8_t *gmix)
+{
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    uint32_t q, off, rem;
+    pi.get(x, q, off, rem);
+    if (rem <= W) return;
+    const uint32_t g = grp_of[x];
+    const uint32_t c = pc_code(dict, pcmin, pcmax, x, q, off);
+    if (c == PC_VAR || c != gchar[g]) gmix[g] = 1;
+}
+
+struct LoadGCount {
+    const uint32_t *gcount;
+    __device__ __forceinline__ uint32_t operator()(size_t g) const { return gcount[g]; }
+};
+// Mixed groups: packed (count of mixed groups, bytes in mixed groups).
+struct LoadMixPair {
+    const uint32_t *gcount;
+    const uint8_t *gmix;
+    __device__ __forceinline__ uint64_t operator()(size_t g) const
+    {
+        return gmix[g] ? ((1ull << 32) | gcount[g]) : 0ull;
+    }
+};
+struct StoreMix {
+    const uint8_t *gmix;
+    const uint32_t *goff;
+    uint32_t *mixidx;
+    uint32_t *delta;
+    __device__ __forceinline__ void operator()(size_t g, uint64_t pre, uint64_t) const
+    {
+        if (!gmix[g]) return;
+        const uint32_t b = (uint32_t)(pre >> 32), mstart = (uint32_t)pre;
+        mixidx[g] = b;
+        delta[b] = goff[g] - mstart;
+    }
+};
+
+// Per-phrase lists of mixed suffixes, in dictionary (phrase, offset) order.
+struct LoadMixEntry {
+    PosInfo pi;
+    uint32_t W;
+    const uint32_t *grp_of;
+    const uint8_t *gmix;
+    __device__ __forceinline__ uint32_t operator()(size_t x) const
+    {
+        uint32_t q, off, rem;
+        pi.get((uint32_t)x, q, off, rem);
+        return (rem > W && gmix[grp_of[x]]) ? 1u : 0u;
+    }
+};
+struct StoreMixEntry {
+    PosInfo pi;
+    const uint8_t *dict;
+    const uint32_t *grp_of, *mixidx;
+    uint32_t *moff;
+    uint32_t *mb;
+    uint16_t *mc;
+    __device__ __forceinline__ void operator()(size_t x, uint32_t pre, uint32_t v) const
+    {
+        uint32_t q, off, rem;
+        pi.get((uint32_t)x, q, off, rem);
+        if (off == 0) moff[q] = pre;
+        if (v) {
+            mb[pre] = mixidx[grp_of[x]];
+            mc[pre] = (uint16_t)(off ? dict[x - 1] : PC_VAR);
+        }
+    }
+};
+
+// Emission order: the last phrase first (its next-suffix rank is -1,
+// K:787-807), then the phrase before each parse suffix in suffix-array order.
+struct Emit {
+    const uint32_t *psa, *pisa, *pid, *moff, *D;
+    uint32_t z;
+    __device__ __forceinline__ uint32_t occ_at(size_t t) const
+    {
+        if (t == 0) return z - 1u;
+        const uint32_t pos0 = pisa[0];
+        const uint32_t r = (uint32_t)t - 1u < pos0 ? (uint32_t)t - 1u : (uint32_t)t;
+        return psa[r] - 1u;
+    }
+};
+struct LoadEmitCount {
+    Emit e;
+    __device__ __forceinline__ uint32_t operator()(size_t t) const
+    {
+        const uint32_t q = e.pid[e.occ_at(t)];
+        return e.moff[q + 1] - e.moff[q];
+    }
+};
+template <typename E>
+struct StoreEmit {
+    Emit e;
+    const uint32_t *mb;
+    const uint16_t *mc;
+    const uint8_t *T;
+    uint32_t n;
+    int W;
+    E *elem;
+    uint32_t cap;          // elements allocated (= bytes in mixed blocks)
+    uint32_t *flags;
+    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t cnt) const
+    {
+        if (!cnt) return;
+        if ((uint64_t)pre + cnt > cap) { atomicOr(flags, ERR_INTERNAL); return; }
+        const uint32_t k = e.occ_at(t);
+        const uint32_t q = e.pid[k];
+        const uint32_t base = e.moff[q];
+        const uint32_t start = k ? e.D[k - 1] - (uint32_t)W + 1u : 0u;
+        const uint32_t prev = preceding_byte(T, n, start);
+        for (uint32_t j = 0; j < cnt; j++) {
+            uint32_t c = mc[base + j];
+            if (c == PC_VAR) c = prev;
+            elem[pre + j] = ((E)mb[base + j] << 8) | (E)c;
+        }
+    }
+};
+
+template <typename E>
+__global__ void k_mixed_scatter(const E *elem, uint32_t M, const uint32_t *delta, uint32_t B, uint8_t *out,
+                                uint32_t n, uint32_t *flags)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    const E e = elem[i];
+    const uint32_t b = (uint32_t)(e >> 8);
+    const uint32_t p = b < B ? i + delta[b] : 0xFFFFFFFFu;
+    if (p < n) out[p] = (uint8_t)(e & 0xFFu);
+    else atomicOr(flags, ERR_INTERNAL);
+}
+
+// Run fill: 4096 output bytes per CTA, 16 per thread (one 16-byte store);
+// bytes of mixed groups are written as 0 and overwritten by the scatter.
+constexpr int RF_THREADS = 256;
+constexpr int RF_TILE = RF_THREADS * 16;
+
+__global__ void __launch_bounds__(RF_THREADS) k_run_fill(uint8_t *out, uint32_t n, const uint32_t *goff, uint32_t G,
+                                                         const uint16_t *gchar, const uint8_t *gmix)
+{
+    __shared__ uint32_t s_off[RF_TILE + 2];
+    __shared__ uint8_t s_chr[RF_TILE + 2];
+    __shared__ uint32_t s_lo, s_hi;
+    const uint32_t base = blockIdx.x * RF_TILE;
+    const uint32_t tile_end = min(base + RF_TILE, n);    // exclusive
+    if (threadIdx.x < 2) {
+        // last group g with goff[g] <= p
+        const uint32_t p = threadIdx.x == 0 ? base : tile_end - 1u;
+        uint32_t lo = 0, hi = G - 1u;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi + 1u) >> 1;
+            if (goff[mid] <= p) lo = mid; else hi = mid - 1u;
+        }
+        if (threadIdx.x == 0) s_lo = lo; else s_hi = lo;
+    }
+    __syncthreads();
+    const uint32_t glo = s_lo, m = s_hi - s_lo + 1u;   // m <= RF_TILE
+    for (uint32_t i = threadIdx.x; i <= m; i += RF_THREADS) {
+        s_off[i] = goff[glo + i];      // goff[G] == n exists
+        if (i < m) s_chr[i] = gmix[glo + i] ? 0 : (uint8_t)gchar[glo + i];
+    }
+    __syncthreads();
+    const uint32_t p0 = base + threadIdx.x * 16u;
+    if (p0 >= tile_end) return;
+    uint32_t lo = 0, hi = m - 1u;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1u) >> 1;
+        if (s_off[mid] <= p0) lo = mid; else hi = mid - 1u;
+    }
+    uint8_t b[16];
+    uint32_t g = lo;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const uint32_t p = p0 + j;
+        while (g + 1u < m && s_off[g + 1u] <= p) g++;
+        b[j] = s_chr[g];
+    }
+    if (p0 + 16u <= n && (((uintptr_t)(out + p0)) & 15u) == 0) {
+        uint4 v;
+        memcpy(&v, b, 16);
+        *(uint4 *)(out + p0) = v;
+    } else {
+        for (int j = 0; j < 16 && p0 + j < n; j++) out[p0 + j] = b[j];
+    }
+}
+
+// Output row of the suffix starting at text position 0 (the "primary index"):
+// its block is the group g0 of phrase 0 taken whole; inside a block the rows
+// follow the rank of the next parse suffix (last phrase: -1, K:787-807).
+struct PrimaryArgs {
+    const uint32_t *pid, *pisa, *doff, *dlen, *grp_of, *goff;
+    uint32_t z;
+    uint32_t *counter;
+};
+__global__ void k_primary_index(PrimaryArgs a)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t q0 = a.pid[0], len0 = a.dlen[q0];
+    const uint32_t g0 = a.grp_of[a.doff[q0]];
+    bool before = false;
+    if (k < a.z && k != 0) {
+        const uint32_t q = a.pid[k], lq = a.dlen[q];
+        if (lq >= len0 && a.grp_of[a.doff[q] + lq - len0] == g0) {
+            const int64_t nr0 = a.z > 1 ? (int64_t)a.pisa[1] : -1;
+            const int64_t nrk = k + 1 < a.z ? (int64_t)a.pisa[k + 1] : -1;
+            before = nrk < nr0;
+        }
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, before);
+    if ((threadIdx.x & 31u) == 0 && m) atomicAdd(a.counter, (uint32_t)__popc(m));
+    if (k == 0) atomicAdd(a.counter, a.goff[g0]);
+}
+
+template <typename E>
+static void mixed_blocks(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, ParseOrder &pord,
+                         const uint32_t *moff, const uint32_t *mb, const uint16_t *mc, const uint32_t *delta,
+                         uint32_t B, uint32_t M, uint8_t *dOut)
+{
+    E *elem = slot<E>(st, S_ELEM0, M);
+    E *elem_alt = slot<E>(st, S_ELEM1, M);
+    Emit e{pord.sa, pord.isa, ph.pid, moff, ph.D, ph.z};
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, ph.z, LoadEmitCount{e},
+                                 StoreEmit<E>{e, mb, mc, dT, n, W, elem, M, st->d_flags}, false,
+                                 (uint32_t *)st->d_scalars);
+    uint32_t *nv = nullptr, *nv2 = nullptr;
+    radix_sort<E, false>(st, elem, elem_alt, nv, nv2, M, 8, 8 + bits_for(B - 1));
+    probe_begin(st, GBWT_PROBE_MIXED_SCATTER);
+    k_mixed_scatter<E><<<grid_for(M, 256), 256, 0, st->stream>>>(elem, M, delta, B, dOut, n, st->d_flags);
+    probe_end(st, GBWT_PROBE_MIXED_SCATTER, (uint64_t)M * (sizeof(E) + 1));
+    after_launch(st);
+}
+
+void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, DictOrder &dord,
+                  ParseOrder &pord, uint8_t *dOut)
+{
+    const uint32_t N = (uint32_t)ph.dict_bytes;
+    PosInfo pi{ph.dphr, ph.doff, ph.dlen};
+    // groups: at most one per dictionary position
+    uint32_t *gcount = slot<uint32_t>(st, S_GCOUNT, N);
+    uint16_t *gchar = slot<uint16_t>(st, S_GCHAR, N);
+    uint32_t *grp_of = slot<uint32_t>(st, S_GRP, N);
+    check_cuda(cudaMemsetAsync(gcount, 0, (size_t)N * 4, st->stream));
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, N, LoadSHead{dord.sa, dord.isa, pi, (uint32_t)W},
+                                 StoreSGroup{dord.sa, pi, (uint32_t)W, ph.dict, ph.occ, ph.pcmin, ph.pcmax, gcount,
+                                             gchar, grp_of},
+                                 true, (uint32_t *)st->d_scalars);
+    fetch_scalars(st, 1);
+    const uint32_t G = (uint32_t)st->h_scalars[0];
+    if (G == 0) throw Error{GBWT_INTERNAL_ERROR};
+    uint8_t *gmix = slot<uint8_t>(st, S_GMIX, G);
+    check_cuda(cudaMemsetAsync(gmix, 0, G, st->stream));
+    k_mark_mixed<<<grid_for(N, 256), 256, 0, st->stream>>>(N, pi, (uint32_t)W, ph.dict, ph.pcmin, ph.pcmax, grp_of,
+                                                           gchar, gmix);
+    after_launch(st);
+    uint32_t *goff = slot<uint32_t>(st, S_GOFF, (size_t)G + 1);
+    device_scan<uint32_t, OpAdd>(st, G, LoadGCount{gcount}, StoreArr<uint32_t>{goff}, false, goff + G);
+    uint32_t *mixidx = slot<uint32_t>(st, S_MIXIDX, G);
+    uint32_t *delta = slot<uint32_t>(st, S_DELTA, G);
+    check_cuda(cudaMemsetAsync(st->d_scalars + 1, 0, 8, st->stream));
+    device_scan<uint64_t, OpAdd>(st, G, LoadMixPair{gcount, gmix}, StoreMix{gmix, goff, mixidx, delta}, false,
+                                 (uint64_t *)(st->d_scalars + 1));
+    check_cuda(cudaMemcpyAsync(st->d_scalars + 2, goff + G, 4, cudaMemcpyDeviceToDevice, st->stream));
+    fetch_scalars(st, 3);
+    const uint32_t B = (uint32_t)(st->h_scalars[1] >> 32);
+    const uint32_t M = (uint32_t)st->h_scalars[1];
+    const uint32_t total = (uint32_t)st->h_scalars[2];
+    if (total != n) throw Error{GBWT_INTERNAL_ERROR};
+    st->stats.s = G;
+    st->stats.mixed_blocks = B;
+    st->stats.mixed_elems = M;
+    stage_mark(st, 4);
+
+    k_primary_index<<<grid_for(ph.z, 256), 256, 0, st->stream>>>(
+        PrimaryArgs{ph.pid, pord.isa, ph.doff, ph.dlen, grp_of, goff, ph.z, st->d_flags + 2});
+    after_launch(st);
+    probe_begin(st, GBWT_PROBE_RUN_FILL);
+    k_run_fill<<<grid_for(n, RF_TILE), RF_THREADS, 0, st->stream>>>(dOut, n, goff, G, gchar, gmix);
+    probe_end(st, GBWT_PROBE_RUN_FILL, (uint64_t)n + 7ull * G);
+    after_launch(st);
+    stage_mark(st, 5);
+    if (B == 0) return;
+
+    // per-phrase mixed-suffix lists
+    uint32_t *moff = slot<uint32_t>(st, S_MOFF, (size_t)ph.d + 1);
+    uint32_t *mb = slot<uint32_t>(st, S_MB, N);
+    uint16_t *mc = slot<uint16_t>(st, S_MC, N);
+    device_scan<uint32_t, OpAdd>(st, N, LoadMixEntry{pi, (uint32_t)W, grp_of, gmix},
+                                 StoreMixEntry{pi, ph.dict, grp_of, mixidx, moff, mb, mc}, false, moff + ph.d);
+    if (B < (1u << 24)) mixed_blocks<uint32_t>(st, dT, n, W, ph, pord, moff, mb, mc, delta, B, M, dOut);
+    else mixed_blocks<uint64_t>(st, dT, n, W, ph, pord, moff, mb, mc, delta, B, M, dOut);
+}
+
+}  // namespace gbwt

@@ -1,0 +1,237 @@
+// pfp_scan.cu -- Karp-Rabin trigger scan (phrase ends) for sm_103a.
+//
+// Semantics follow Compute_D1/D2/D3 of the reference
+// (Prefix_Free_Parsing_W=5_P=16_kommentiert.cu, "K", K:443-576):
+//   window s (s+W-1 < n) triggers when
+//     h(s) = sum_{k<W} T[s+W-1-k] * (2^k mod P)  (mod P)  == 0
+//   or when T[s..s+W-1] == T[0..W-1]; window 0 never triggers.
+//   D lists the triggering windows' last positions, then n+W-1.
+//
+// GB300 layout: a CTA owns 4096 window starts; the 4096+W-1 bytes it needs
+// are staged in shared memory with 16-byte loads; every thread pulls its 16
+// windows (+ W-1 halo) into registers with 16-byte shared loads and rolls
+// the hash mod P (h(s+1) = 2h(s) - T[s]*2^W + T[s+W]).  The first-word test
+// rolls an exact packed register for W <= 8 and a 64-bit polynomial
+// fingerprint (verified byte by byte on a hit) for longer windows.  Trigger
+// positions are compacted with popc + a CTA scan; the count pass also
+// validates the input bytes (K:130-132) without trapping.
+#include "prims.cuh"
+
+namespace gbwt {
+
+constexpr int TS_THREADS = 256;
+constexpr int TS_PER_THREAD = 16;
+constexpr int TS_TILE = TS_THREADS * TS_PER_THREAD;
+constexpr int TS_MAXW = 64;
+constexpr uint64_t FP_BASE = 0x100000001B3ull;
+
+struct ScanArgs {
+    const uint8_t *T;
+    uint32_t n;
+    int W;
+    int P;
+    uint32_t wW;        // 2^W mod P
+    uint32_t hi;        // largest valid byte (254, or 15 for the small alphabet)
+    uint32_t *flags;    // error bits
+};
+
+__device__ __forceinline__ uint32_t bget(const uint32_t *w, int i) { return (w[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
+
+// Stage bytes [base, base + TS_TILE + W - 1) of T into s (zero past n).
+__device__ __forceinline__ void stage_tile(const ScanArgs &a, uint8_t *s, size_t base, int halo16)
+{
+    const bool aligned = (((uintptr_t)a.T) & 15u) == 0;
+    const int nvec = TS_TILE / 16 + halo16;
+    for (int v = threadIdx.x; v < nvec; v += TS_THREADS) {
+        size_t p = base + (size_t)v * 16;
+        uint4 val;
+        if (aligned && p + 16 <= a.n) {
+            val = __ldg((const uint4 *)(a.T + p));
+        } else {
+            uint8_t b[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) b[j] = (p + j < a.n) ? __ldg(a.T + p + j) : 0;
+            memcpy(&val, b, 16);
+        }
+        *(uint4 *)(s + (size_t)v * 16) = val;
+    }
+}
+
+// One tile: returns this thread's 16-bit trigger mask and checks bytes.
+template <int WT, int PT>
+__device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8_t *s, const uint8_t *s_fw,
+                                                  uint64_t fw_packed, uint64_t fp0, uint64_t fp_pow,
+                                                  size_t base, bool check_bytes)
+{
+    constexpr int NB = TS_PER_THREAD + (WT > 0 ? WT : TS_MAXW) - 1;   // bytes needed
+    constexpr int NV = (NB + 15) / 16;                                 // uint4 loads
+    const int W = WT > 0 ? WT : a.W;
+    const uint32_t P = PT > 0 ? (uint32_t)PT : (uint32_t)a.P;
+    const size_t s0 = base + (size_t)threadIdx.x * TS_PER_THREAD;
+
+    uint32_t w[NV * 4];
+    const uint8_t *src = s + (size_t)threadIdx.x * TS_PER_THREAD;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        uint4 q = *(const uint4 *)(src + v * 16);
+        w[v * 4 + 0] = q.x; w[v * 4 + 1] = q.y; w[v * 4 + 2] = q.z; w[v * 4 + 3] = q.w;
+    }
+
+    if (check_bytes) {
+        bool bad = false, small_bad = false;
+#pragma unroll
+        for (int j = 0; j < TS_PER_THREAD; j++) {
+            uint32_t c = bget(w, j);
+            if (s0 + j < a.n) {
+                bad |= (c < 2u) || (c == 255u);
+                small_bad |= (c > a.hi);
+            }
+        }
+        if (bad) atomicOr(a.flags, ERR_BAD_BYTE);
+        else if (small_bad) atomicOr(a.flags, ERR_SMALL_RANGE);
+    }
+
+    if (a.n < (uint32_t)W) return 0;
+    const size_t last_valid = (size_t)a.n - (size_t)W;   // last window start
+    if (s0 > last_valid) return 0;
+
+    // hash of the first window: sum b[i] * 2^(W-1-i) mod P
+    uint32_t h = 0;
+    {
+        uint32_t pw = 1;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int i = (WT > 0 ? WT : TS_MAXW) - 1; i >= 0; i--) {
+            if (WT == 0 && i >= W) continue;
+            acc += bget(w, i) * pw;
+            pw = (pw * 2u) % P;
+            if (WT == 0 || WT > 16) acc %= P;
+        }
+        h = acc % P;
+    }
+    // first-word test state
+    uint64_t reg = 0, fp = 0;
+    if (WT > 0 && WT <= 8) {
+#pragma unroll
+        for (int i = 0; i < (WT > 0 ? WT : 1); i++) reg = (reg << 8) | bget(w, i);
+    } else {
+#pragma unroll
+        for (int i = 0; i < (WT > 0 ? WT : TS_MAXW); i++) {
+            if (WT == 0 && i >= W) break;
+            fp = fp * FP_BASE + bget(w, i);
+        }
+    }
+    const uint64_t regmask = (WT > 0 && WT < 8) ? ((1ull << (8 * (WT > 0 ? WT : 1))) - 1ull) : ~0ull;
+
+    uint32_t mask = 0;
+#pragma unroll
+    for (int j = 0; j < TS_PER_THREAD; j++) {
+        const size_t sj = s0 + j;
+        bool eq;
+        if (WT > 0 && WT <= 8) {
+            eq = reg == fw_packed;
+        } else {
+            eq = false;
+            if (fp == fp0) {
+                eq = true;
+                for (int i = 0; i < W; i++)
+                    if (s[sj - base + i] != s_fw[i]) { eq = false; break; }
+            }
+        }
+        if (sj >= 1 && sj <= last_valid && (h == 0 || eq)) mask |= 1u << j;
+        if (j + 1 < TS_PER_THREAD) {
+            const uint32_t out = bget(w, j), in = bget(w, j + W);
+            h = (2u * h + in + 256u * P - out * a.wW) % P;
+            if (WT > 0 && WT <= 8) reg = ((reg << 8) | in) & regmask;
+            else fp = fp * FP_BASE - (uint64_t)out * fp_pow + in;
+        }
+    }
+    return mask;
+}
+
+template <int WT, int PT, bool WRITE>
+__global__ void __launch_bounds__(TS_THREADS) k_trigger(ScanArgs a, uint32_t *counts, const uint32_t *offsets,
+                                                        uint32_t *D)
+{
+    __shared__ __align__(16) uint8_t s[TS_TILE + TS_MAXW + 64];
+    __shared__ uint8_t s_fw[TS_MAXW];
+    __shared__ uint32_t s_warp[32];
+    const int W = WT > 0 ? WT : a.W;
+    const size_t base = (size_t)blockIdx.x * TS_TILE;
+    const int halo16 = (W - 1 + 15) / 16 + 1;
+    stage_tile(a, s, base, halo16);
+    if (threadIdx.x < (unsigned)W) s_fw[threadIdx.x] = threadIdx.x < a.n ? __ldg(a.T + threadIdx.x) : 1;
+    __syncthreads();
+
+    uint64_t fw_packed = 0, fp0 = 0, fp_pow = 1;
+    for (int i = 0; i < W; i++) {
+        fw_packed = (fw_packed << 8) | s_fw[i];
+        fp0 = fp0 * FP_BASE + s_fw[i];
+        fp_pow *= FP_BASE;
+    }
+    uint32_t mask = tile_triggers<WT, PT>(a, s, s_fw, fw_packed, fp0, fp_pow, base, !WRITE);
+    uint32_t cnt = __popc(mask), total;
+    uint32_t ex = block_excl_scan<uint32_t, OpAdd>(cnt, total, OpAdd(), s_warp);
+    if (!WRITE) {
+        if (threadIdx.x == 0) counts[blockIdx.x] = total;
+        return;
+    }
+    uint32_t o = offsets[blockIdx.x] + ex;
+    const uint32_t s0 = (uint32_t)(base + (size_t)threadIdx.x * TS_PER_THREAD);
+    while (mask) {
+        int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        D[o++] = s0 + (uint32_t)j + (uint32_t)W - 1u;
+    }
+}
+
+template <int WT, int PT>
+static void launch_pair(Storage *st, const ScanArgs &a, unsigned blocks, uint32_t *counts, uint32_t *&D)
+{
+    probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
+    k_trigger<WT, PT, false><<<blocks, TS_THREADS, 0, st->stream>>>(a, counts, nullptr, nullptr);
+    probe_end(st, GBWT_PROBE_TRIGGER_SCAN, a.n);
+    after_launch(st);
+    // exclusive scan of block counts; total -> d_scalars[0]
+    uint32_t *tot = (uint32_t *)st->d_scalars;
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, blocks, LoadArr<uint32_t>{counts}, StoreArr<uint32_t>{counts}, false, tot);
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 1, a.flags, 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars, st->d_scalars, 8, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    uint32_t flags = (uint32_t)st->h_scalars[1];
+    if (flags & ERR_BAD_BYTE) throw Error{GBWT_BAD_PARAMETER};
+    if (flags & ERR_SMALL_RANGE) throw Error{GBWT_UNSUPPORTED_INPUT};
+    uint32_t c = (uint32_t)(st->h_scalars[0] & 0xFFFFFFFFu);
+    D = slot<uint32_t>(st, S_D, (size_t)c + 1);
+    probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
+    k_trigger<WT, PT, true><<<blocks, TS_THREADS, 0, st->stream>>>(a, nullptr, counts, D);
+    probe_end(st, GBWT_PROBE_TRIGGER_SCAN, (uint64_t)a.n + 4ull * c);
+    after_launch(st);
+    k_set_u32<<<1, 1, 0, st->stream>>>(D + c, a.n + (uint32_t)a.W - 1u);
+    after_launch(st);
+    st->h_scalars[0] = c;
+}
+
+uint32_t run_trigger_scan(Storage *st, const uint8_t *dT, uint32_t n, int W, int P, bool small, uint32_t *&D)
+{
+    ScanArgs a;
+    a.T = dT; a.n = n; a.W = W; a.P = P;
+    uint32_t wW = 1;
+    for (int i = 0; i < W; i++) wW = (wW * 2u) % (uint32_t)P;
+    a.wW = wW;
+    a.hi = small ? 15u : 254u;
+    a.flags = st->d_flags;
+    unsigned blocks = grid_for(n, TS_TILE);
+    uint32_t *counts = slot<uint32_t>(st, S_TMP0, blocks + 1);
+    if (W == 5 && P == 16) launch_pair<5, 16>(st, a, blocks, counts, D);
+    else if (W == 5 && P == 11) launch_pair<5, 11>(st, a, blocks, counts, D);
+    else if (W == 5 && P == 13) launch_pair<5, 13>(st, a, blocks, counts, D);
+    else if (W == 5 && P == 14) launch_pair<5, 14>(st, a, blocks, counts, D);
+    else if (W == 5 && P == 23) launch_pair<5, 23>(st, a, blocks, counts, D);
+    else if (W == 35 && P == 81) launch_pair<35, 81>(st, a, blocks, counts, D);
+    else launch_pair<0, 0>(st, a, blocks, counts, D);
+    return (uint32_t)st->h_scalars[0] + 1u;
+}
+
+}  // namespace gbwt

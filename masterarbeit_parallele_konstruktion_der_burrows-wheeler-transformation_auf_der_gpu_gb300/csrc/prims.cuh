@@ -1,0 +1,335 @@
+// prims.cuh -- device-wide scan and stable LSD radix sort (sm_103a).
+//
+// Scan: reduce-then-scan over tiles of 4096 items, with functor loads and
+// stores so that flags, compaction and segmented heads are computed on the
+// fly instead of being materialised.
+//
+// Radix sort: stable LSD passes over 8-bit digits.  Each pass runs a tile
+// histogram (warp-aggregated shared atomics), a digit-major exclusive scan of
+// the tile histograms, and a scatter kernel that ranks keys inside each warp
+// with __match_any_sync multisplit, reorders the tile in shared memory and
+// writes each digit's run with consecutive addresses.
+#pragma once
+#include "gbwt_internal.cuh"
+
+namespace gbwt {
+
+constexpr int SC_THREADS = 256;
+constexpr int SC_ITEMS = 16;
+constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+
+struct OpAdd {
+    template <typename T> __device__ __forceinline__ T operator()(T a, T b) const { return a + b; }
+};
+struct OpMax {
+    template <typename T> __device__ __forceinline__ T operator()(T a, T b) const { return a > b ? a : b; }
+};
+// Component-wise max of the two 32-bit halves of a 64-bit word.
+struct OpMax2 {
+    __device__ __forceinline__ uint64_t operator()(uint64_t a, uint64_t b) const {
+        uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+        uint32_t al = (uint32_t)a, bl = (uint32_t)b;
+        return ((uint64_t)(ah > bh ? ah : bh) << 32) | (al > bl ? al : bl);
+    }
+};
+
+// Block-wide exclusive scan (identity 0); `total` receives the block total.
+template <typename T, typename Op>
+__device__ __forceinline__ T block_excl_scan(T v, T &total, Op op, T *s_warp /*[32]*/)
+{
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned nw = (blockDim.x + 31) >> 5;
+    T x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (unsigned)o) x = op(y, x);
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nw ? s_warp[lane] : T(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            T y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (unsigned)o) w = op(y, w);
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    T wp = warp ? s_warp[warp - 1] : T(0);
+    total = s_warp[nw - 1];
+    T xe = __shfl_up_sync(0xFFFFFFFFu, x, 1);
+    if (lane == 0) xe = T(0);
+    __syncthreads();
+    return op(wp, xe);
+}
+
+// ---- scan kernels ---------------------------------------------------
+template <typename T, typename Op, typename Load>
+__global__ void __launch_bounds__(SC_THREADS) k_scan_reduce(Load load, size_t n, T *partial)
+{
+    __shared__ T s_warp[32];
+    Op op;
+    size_t base = (size_t)blockIdx.x * SC_TILE;
+    T acc = T(0);
+#pragma unroll 4
+    for (int j = 0; j < SC_ITEMS; j++) {
+        size_t i = base + (size_t)j * SC_THREADS + threadIdx.x;
+        if (i < n) acc = op(acc, load(i));
+    }
+    T total;
+    block_excl_scan<T, Op>(acc, total, op, s_warp);
+    if (threadIdx.x == 0) partial[blockIdx.x] = total;
+}
+
+template <typename T, typename Op, typename Load, typename Store>
+__global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store, size_t n,
+                                                          const T *partial, bool inclusive,
+                                                          T *total_out)
+{
+    __shared__ T s_tile[SC_TILE];
+    __shared__ T s_warp[32];
+    Op op;
+    size_t base = (size_t)blockIdx.x * SC_TILE;
+    // striped (coalesced) loads into shared memory, then blocked reads
+#pragma unroll 4
+    for (int j = 0; j < SC_ITEMS; j++) {
+        size_t i = base + (size_t)j * SC_THREADS + threadIdx.x;
+        s_tile[j * SC_THREADS + threadIdx.x] = i < n ? load(i) : T(0);
+    }
+    __syncthreads();
+    T v[SC_ITEMS];
+    T sum = T(0);
+#pragma unroll
+    for (int j = 0; j < SC_ITEMS; j++) {
+        v[j] = s_tile[threadIdx.x * SC_ITEMS + j];
+        sum = op(sum, v[j]);
+    }
+    T total;
+    T ex = block_excl_scan<T, Op>(sum, total, op, s_warp);
+    T run = partial ? op(partial[blockIdx.x], ex) : ex;
+    size_t i0 = base + (size_t)threadIdx.x * SC_ITEMS;
+#pragma unroll
+    for (int j = 0; j < SC_ITEMS; j++) {
+        size_t i = i0 + j;
+        if (i < n) {
+            T inc = op(run, v[j]);
+            store(i, inclusive ? inc : run, v[j]);
+            if (total_out && i == n - 1) *total_out = inc;
+            run = inc;
+        }
+    }
+}
+
+template <typename T>
+struct LoadArr {
+    const T *a;
+    __device__ __forceinline__ T operator()(size_t i) const { return a[i]; }
+};
+template <typename T>
+struct StoreArr {
+    T *a;
+    __device__ __forceinline__ void operator()(size_t i, T pre, T) const { a[i] = pre; }
+};
+
+// In-place exclusive scan of a plain array (used for partials and histograms).
+template <typename T, typename Op>
+void scan_array_excl(Storage *st, T *a, size_t m, int depth)
+{
+    if (m == 0) return;
+    size_t tiles = (m + SC_TILE - 1) / SC_TILE;
+    if (tiles == 1) {
+        k_scan_down<T, Op><<<1, SC_THREADS, 0, st->stream>>>(LoadArr<T>{a}, StoreArr<T>{a}, m,
+                                                              (const T *)nullptr, false, (T *)nullptr);
+        after_launch(st);
+        return;
+    }
+    if (depth >= 3) throw Error{GBWT_INTERNAL_ERROR};
+    T *part = slot<T>(st, S_SCAN1 + depth, tiles);
+    k_scan_reduce<T, Op><<<(unsigned)tiles, SC_THREADS, 0, st->stream>>>(LoadArr<T>{a}, m, part);
+    after_launch(st);
+    scan_array_excl<T, Op>(st, part, tiles, depth + 1);
+    k_scan_down<T, Op><<<(unsigned)tiles, SC_THREADS, 0, st->stream>>>(LoadArr<T>{a}, StoreArr<T>{a}, m,
+                                                                        part, false, (T *)nullptr);
+    after_launch(st);
+}
+
+// Scan of load(i), i in [0,n): store(i, prefix, value) is called with the
+// exclusive (or inclusive) prefix.  The total is written to *total_dev when
+// given (device pointer; left untouched for n == 0).
+template <typename T, typename Op, typename Load, typename Store>
+void device_scan(Storage *st, size_t n, Load load, Store store, bool inclusive, T *total_dev)
+{
+    if (n == 0) return;
+    size_t tiles = (n + SC_TILE - 1) / SC_TILE;
+    T *part = nullptr;
+    if (tiles > 1) {
+        part = slot<T>(st, S_SCAN0, tiles);
+        k_scan_reduce<T, Op><<<(unsigned)tiles, SC_THREADS, 0, st->stream>>>(load, n, part);
+        after_launch(st);
+        scan_array_excl<T, Op>(st, part, tiles, 0);
+    }
+    k_scan_down<T, Op><<<(unsigned)tiles, SC_THREADS, 0, st->stream>>>(load, store, n, part, inclusive,
+                                                                        total_dev);
+    after_launch(st);
+}
+
+// ---------------------------------------------------------------------
+// Stable LSD radix sort
+// ---------------------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+template <typename K>
+__device__ __forceinline__ uint32_t rs_digit(K k, int shift, uint32_t mask)
+{
+    return (uint32_t)(k >> shift) & mask;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__ keys, uint32_t n, int shift,
+                                                           uint32_t mask, uint32_t *__restrict__ tile_hist,
+                                                           uint32_t num_tiles)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+    for (int j = 0; j < RS_ITEMS; j++) {
+        size_t i = base + (size_t)j * RS_THREADS + threadIdx.x;
+        bool valid = i < n;
+        uint32_t d = valid ? rs_digit(keys[i], shift, mask) : 0xFFFFFFFFu;
+        unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    tile_hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+template <typename K, bool HAS_VAL>
+constexpr size_t rs_smem_bytes()
+{
+    return (size_t)RS_TILE * sizeof(K) + (HAS_VAL ? (size_t)RS_TILE * 4 : 0) + (size_t)RS_WARPS * 256 * 4 +
+           256 * 4 * 2 + 32 * 4;
+}
+
+template <typename K, bool HAS_VAL>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict__ kin, K *__restrict__ kout,
+                                                             const uint32_t *__restrict__ vin,
+                                                             uint32_t *__restrict__ vout, uint32_t n, int shift,
+                                                             uint32_t mask, const uint32_t *__restrict__ tile_off,
+                                                             uint32_t num_tiles)
+{
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    K *s_k = (K *)rs_smem;
+    uint32_t *s_v = (uint32_t *)(s_k + RS_TILE);
+    uint32_t *s_wh = HAS_VAL ? s_v + RS_TILE : s_v;
+    uint32_t *s_dstart = s_wh + RS_WARPS * 256;
+    uint32_t *s_goff = s_dstart + 256;
+    uint32_t *s_scan = s_goff + 256;
+
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) s_wh[i] = 0;
+    __syncthreads();
+
+    const size_t tile_base = (size_t)blockIdx.x * RS_TILE;
+    const size_t wbase = tile_base + (size_t)warp * (RS_ITEMS * 32);
+    K k[RS_ITEMS];
+    uint32_t v[RS_ITEMS];
+    uint32_t rk[RS_ITEMS];
+    uint32_t dg[RS_ITEMS];
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        size_t idx = wbase + (size_t)i * 32 + lane;
+        bool valid = idx < n;
+        k[i] = valid ? kin[idx] : K(0);
+        if (HAS_VAL) v[i] = valid ? vin[idx] : 0u;
+        dg[i] = valid ? rs_digit(k[i], shift, mask) : 0xFFFFFFFFu;
+    }
+    uint32_t *wh = s_wh + warp * 256;
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        uint32_t d = dg[i];
+        unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        unsigned leader = (unsigned)(__ffs(peers) - 1);
+        uint32_t prior = 0;
+        if (lane == leader && d != 0xFFFFFFFFu) {
+            prior = wh[d];
+            wh[d] = prior + (uint32_t)__popc(peers);
+        }
+        prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
+        rk[i] = prior + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const uint32_t d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            uint32_t c = s_wh[w * 256 + d];
+            s_wh[w * 256 + d] = run;
+            run += c;
+        }
+        uint32_t total;
+        uint32_t ex = block_excl_scan<uint32_t, OpAdd>(run, total, OpAdd(), s_scan);
+        s_dstart[d] = ex;
+        s_goff[d] = tile_off[(size_t)d * num_tiles + blockIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        if (dg[i] != 0xFFFFFFFFu) {
+            uint32_t lp = s_dstart[dg[i]] + s_wh[warp * 256 + dg[i]] + rk[i];
+            s_k[lp] = k[i];
+            if (HAS_VAL) s_v[lp] = v[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = (uint32_t)(((size_t)n - tile_base) < (size_t)RS_TILE ? ((size_t)n - tile_base) : RS_TILE);
+    for (uint32_t j = threadIdx.x; j < tile_n; j += RS_THREADS) {
+        K kk = s_k[j];
+        uint32_t d = rs_digit(kk, shift, mask);
+        size_t g = (size_t)s_goff[d] + (j - s_dstart[d]);
+        kout[g] = kk;
+        if (HAS_VAL) vout[g] = s_v[j];
+    }
+}
+
+// Sorts (keys, vals) stably by bits [begin_bit, end_bit).  On return `keys`
+// and `vals` point at the sorted data (the *_alt buffers hold garbage).
+template <typename K, bool HAS_VAL>
+void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *&vals_alt, uint32_t n,
+                int begin_bit, int end_bit)
+{
+    if (n <= 1 || end_bit <= begin_bit) return;
+    static bool attr_set = false;
+    constexpr size_t smem = rs_smem_bytes<K, HAS_VAL>();
+    if (!attr_set) {
+        check_cuda(cudaFuncSetAttribute(k_rs_downsweep<K, HAS_VAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        attr_set = true;
+    }
+    uint32_t num_tiles = (uint32_t)((n + RS_TILE - 1) / RS_TILE);
+    uint32_t *hist = slot<uint32_t>(st, S_RSHIST, (size_t)256 * num_tiles);
+    for (int shift = begin_bit; shift < end_bit; shift += 8) {
+        int bits = end_bit - shift < 8 ? end_bit - shift : 8;
+        uint32_t mask = (1u << bits) - 1u;
+        k_rs_upsweep<K><<<num_tiles, RS_THREADS, 0, st->stream>>>(keys, n, shift, mask, hist, num_tiles);
+        after_launch(st);
+        scan_array_excl<uint32_t, OpAdd>(st, hist, (size_t)256 * num_tiles, 0);
+        probe_begin(st, GBWT_PROBE_RADIX_SCATTER);
+        k_rs_downsweep<K, HAS_VAL><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt, n,
+                                                                                shift, mask, hist, num_tiles);
+        probe_end(st, GBWT_PROBE_RADIX_SCATTER, (uint64_t)n * 2 * (sizeof(K) + (HAS_VAL ? 4 : 0)));
+        after_launch(st);
+        K *t = keys; keys = keys_alt; keys_alt = t;
+        if (HAS_VAL) { uint32_t *u = vals; vals = vals_alt; vals_alt = u; }
+    }
+}
+
+}  // namespace gbwt
