@@ -15,7 +15,10 @@
 //
 // Invariant of round h: isa[x] is the first sorted position of x's group of
 // equal h-prefixes; groups are finished when they are singletons or when
-// their common string ends within h symbols.  Keys are (group, isa[x+h]+1)
+// their common string ends within h symbols.  Every group is uniform in
+// whether its strings end within h symbols: the initial keys encode it
+// (dictionary: an explicit bit; parse: the unique last phrase), and a round
+// keyed on isa[x+h] inherits it from the groups of x+h.  Keys are (group, isa[x+h]+1)
 // sorted with the project's stable LSD radix sort; group starts and new heads
 // come from one component-wise max-scan.
 #include "prims.cuh"
@@ -211,8 +214,13 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     return rounds;
 }
 
-// Initial dictionary keys: the next 8 bytes (or 16 four-bit symbols with the
-// small alphabet) of the phrase suffix, zero past the phrase end.
+// Initial dictionary keys: the next h0 = 7 bytes (or 15 four-bit symbols with
+// the small alphabet) of the phrase suffix, zero past the phrase end, then one
+// bit "the suffix continues past h0".  The bit keeps every group uniform in
+// whether its strings end within h0 symbols: without it a suffix of exactly
+// h0 symbols would tie with longer suffixes sharing those symbols.
+constexpr uint32_t DICT_H0 = 7, DICT_H0_SMALL = 15;
+
 __global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, bool small, uint64_t *keys)
 {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -221,10 +229,13 @@ __global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, bool s
     uint64_t key = 0;
     if (small) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) key = (key << 4) | (uint64_t)((uint32_t)i < r ? (dict[x + i] & 15u) : 0u);
+        for (int i = 0; i < (int)DICT_H0_SMALL; i++)
+            key = (key << 4) | (uint64_t)((uint32_t)i < r ? (dict[x + i] & 15u) : 0u);
+        key = (key << 1) | (r > DICT_H0_SMALL ? 1u : 0u);
     } else {
 #pragma unroll
-        for (int i = 0; i < 8; i++) key = (key << 8) | (uint64_t)((uint32_t)i < r ? dict[x + i] : 0u);
+        for (int i = 0; i < (int)DICT_H0; i++) key = (key << 8) | (uint64_t)((uint32_t)i < r ? dict[x + i] : 0u);
+        key = (key << 1) | (r > DICT_H0 ? 1u : 0u);
     }
     keys[x] = key;
 }
@@ -259,7 +270,7 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
     after_launch(st);
     dord.isa = slot<uint32_t>(st, S_ISA, N);
     dord.sa = slot<uint32_t>(st, S_SA, N);
-    dord.rounds = prefix_doubling(st, N, 64, small ? 16u : 8u, rem, dord.isa, dord.sa);
+    dord.rounds = prefix_doubling(st, N, small ? 61 : 57, small ? DICT_H0_SMALL : DICT_H0, rem, dord.isa, dord.sa);
     dord.lexrank = slot<uint32_t>(st, S_LEXRANK, ph.d);
     device_scan<uint32_t, OpAdd>(st, N, LoadIsStart{dord.sa, ph.dphr, ph.doff},
                                  StoreLexRank{dord.sa, ph.dphr, dord.lexrank}, false, (uint32_t *)nullptr);
