@@ -88,7 +88,7 @@ class ClockSampler:
             self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{self.gpu}.csv")
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -308,7 +308,7 @@ def traffic_per_launch(per_launch_bytes):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbwt", choices=["gbwt", "reference"])
     ap.add_argument("--cpu-sample-mib", type=int, default=16)

@@ -30,7 +30,7 @@ enum Slot : int {
     S_GCOUNT, S_GCHAR, S_GMIX, S_GOFF, S_GRP, S_MOFF, S_MB, S_MC, S_MIXIDX, S_DELTA,
     S_ELEM0, S_ELEM1,
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
-    S_TMP0, S_TMP1, S_TMP2,
+    S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG,
     S_NUM
 };
 
@@ -170,6 +170,7 @@ struct Phrases {
     uint64_t dict_bytes = 0;
     const uint32_t *D = nullptr;       // [z] phrase end positions
     uint32_t *pid = nullptr;           // [z] distinct id per occurrence
+    uint32_t *pidpc = nullptr;         // [z] id << 8 | preceding byte (d < 2^24), else null
     uint32_t *dlen = nullptr;          // [d] length of distinct phrase
     uint32_t *doff = nullptr;          // [d+1] offset in dictionary buffer
     uint32_t *occ = nullptr;           // [d] occurrences

@@ -160,53 +160,88 @@ struct Emit {
         return psa[r] - 1u;
     }
 };
-struct LoadEmitCount {
-    Emit e;
-    __device__ __forceinline__ uint32_t operator()(size_t t) const
-    {
-        const uint32_t q = e.pid[e.occ_at(t)];
-        return e.moff[q + 1] - e.moff[q];
-    }
-};
-template <typename E>
-struct StoreEmit {
-    Emit e;
-    const uint32_t *mb;
-    const uint16_t *mc;
-    const uint8_t *T;
-    uint32_t n;
-    int W;
-    E *elem;
-    uint32_t cap;          // elements allocated (= bytes in mixed blocks)
-    uint32_t *flags;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t cnt) const
-    {
-        if (!cnt) return;
-        if ((uint64_t)pre + cnt > cap) { atomicOr(flags, ERR_INTERNAL); return; }
-        const uint32_t k = e.occ_at(t);
-        const uint32_t q = e.pid[k];
-        const uint32_t base = e.moff[q];
-        const uint32_t start = k ? e.D[k - 1] - (uint32_t)W + 1u : 0u;
-        const uint32_t prev = preceding_byte(T, n, start);
-        for (uint32_t j = 0; j < cnt; j++) {
-            uint32_t c = mc[base + j];
-            if (c == PC_VAR) c = prev;
-            elem[pre + j] = ((E)mb[base + j] << 8) | (E)c;
-        }
-    }
-};
 
+// Per emission slot t: phrase id, number of mixed elements and the byte
+// preceding the occurrence (the random gathers happen once, here).
+__global__ void k_emit_prep(Emit e, const uint32_t *pidpc, const uint8_t *T, uint32_t n, int W, uint32_t *emq,
+                            uint8_t *emp, uint32_t *ecnt)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= e.z) return;
+    const uint32_t k = e.occ_at(t);
+    uint32_t q, prev;
+    if (pidpc) {                      // one gather: id and preceding byte packed
+        const uint32_t v = pidpc[k];
+        q = v >> 8;
+        prev = v & 0xFFu;
+    } else {
+        q = e.pid[k];
+        const uint32_t start = k ? e.D[k - 1] - (uint32_t)W + 1u : 0u;
+        prev = preceding_byte(T, n, start);
+    }
+    emq[t] = q;
+    emp[t] = (uint8_t)prev;
+    ecnt[t] = e.moff[q + 1] - e.moff[q];
+}
+
+// 256 emission slots per CTA; the CTA writes its contiguous output range
+// with consecutive threads on consecutive elements.
+constexpr int EM_T = 256;
+template <typename E>
+__global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff, const uint32_t *emq,
+                                               const uint8_t *emp, const uint32_t *moff, const uint32_t *mb,
+                                               const uint16_t *mc, E *elem, uint32_t cap, uint32_t *flags)
+{
+    __shared__ uint32_t s_off[EM_T + 1];
+    __shared__ uint32_t s_base[EM_T];
+    __shared__ uint8_t s_prev[EM_T];
+    const uint32_t t0 = blockIdx.x * EM_T;
+    const uint32_t tn = min((uint32_t)EM_T, z - t0);
+    if (threadIdx.x < tn) {
+        const uint32_t t = t0 + threadIdx.x;
+        s_off[threadIdx.x] = eoff[t];
+        s_base[threadIdx.x] = moff[emq[t]];
+        s_prev[threadIdx.x] = emp[t];
+    }
+    if (threadIdx.x == 0) s_off[tn] = eoff[t0 + tn];
+    __syncthreads();
+    const uint32_t o0 = s_off[0], cnt = s_off[tn] - o0;
+    if ((uint64_t)o0 + cnt > cap) {
+        if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL);
+        return;
+    }
+    for (uint32_t e = threadIdx.x; e < cnt; e += EM_T) {
+        const uint32_t o = o0 + e;
+        uint32_t lo = 0, hi = tn - 1u;            // last i with s_off[i] <= o
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1u) >> 1;
+            if (s_off[mid] <= o) lo = mid; else hi = mid - 1u;
+        }
+        const uint32_t j = s_base[lo] + (o - s_off[lo]);
+        uint32_t c = mc[j];
+        if (c == PC_VAR) c = s_prev[lo];
+        elem[o] = ((E)mb[j] << 8) | (E)c;
+    }
+}
+
+// 4 sorted elements per thread; consecutive elements of one block land on
+// consecutive output bytes.
 template <typename E>
 __global__ void k_mixed_scatter(const E *elem, uint32_t M, const uint32_t *delta, uint32_t B, uint8_t *out,
                                 uint32_t n, uint32_t *flags)
 {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    const E e = elem[i];
-    const uint32_t b = (uint32_t)(e >> 8);
-    const uint32_t p = b < B ? i + delta[b] : 0xFFFFFFFFu;
-    if (p < n) out[p] = (uint8_t)(e & 0xFFu);
-    else atomicOr(flags, ERR_INTERNAL);
+    const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+    if (i0 >= M) return;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; j++) {
+        const uint32_t i = i0 + j;
+        if (i >= M) break;
+        const E e = elem[i];
+        const uint32_t b = (uint32_t)(e >> 8);
+        const uint32_t p = b < B ? i + delta[b] : 0xFFFFFFFFu;
+        if (p < n) out[p] = (uint8_t)(e & 0xFFu);
+        else atomicOr(flags, ERR_INTERNAL);
+    }
 }
 
 // Run fill: 4096 output bytes per CTA, 16 per thread (one 16-byte store);
@@ -214,23 +249,32 @@ __global__ void k_mixed_scatter(const E *elem, uint32_t M, const uint32_t *delta
 constexpr int RF_THREADS = 256;
 constexpr int RF_TILE = RF_THREADS * 16;
 
+// tile_first[t] = the group containing output position t*RF_TILE.
+__global__ void k_tile_first(const uint32_t *goff, uint32_t G, uint32_t *tile_first)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const uint32_t t0 = (goff[g] + RF_TILE - 1) / RF_TILE, t1 = (goff[g + 1] + RF_TILE - 1) / RF_TILE;
+    for (uint32_t t = t0; t < t1; t++) tile_first[t] = g;
+}
+
 __global__ void __launch_bounds__(RF_THREADS) k_run_fill(uint8_t *out, uint32_t n, const uint32_t *goff, uint32_t G,
-                                                         const uint16_t *gchar, const uint8_t *gmix)
+                                                         const uint16_t *gchar, const uint8_t *gmix,
+                                                         const uint32_t *tile_first)
 {
     __shared__ uint32_t s_off[RF_TILE + 2];
     __shared__ uint8_t s_chr[RF_TILE + 2];
     __shared__ uint32_t s_lo, s_hi;
     const uint32_t base = blockIdx.x * RF_TILE;
     const uint32_t tile_end = min(base + RF_TILE, n);    // exclusive
-    if (threadIdx.x < 2) {
-        // last group g with goff[g] <= p
-        const uint32_t p = threadIdx.x == 0 ? base : tile_end - 1u;
-        uint32_t lo = 0, hi = G - 1u;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi + 1u) >> 1;
-            if (goff[mid] <= p) lo = mid; else hi = mid - 1u;
+    if (threadIdx.x == 0) {
+        s_lo = tile_first[blockIdx.x];
+        uint32_t hi = G - 1u;                            // group containing tile_end - 1
+        if (tile_end < n) {
+            hi = tile_first[blockIdx.x + 1];
+            if (goff[hi] == tile_end) hi--;
         }
-        if (threadIdx.x == 0) s_lo = lo; else s_hi = lo;
+        s_hi = hi;
     }
     __syncthreads();
     const uint32_t glo = s_lo, m = s_hi - s_lo + 1u;   // m <= RF_TILE
@@ -297,15 +341,21 @@ static void mixed_blocks(Storage *st, const uint8_t *dT, uint32_t n, int W, Phra
 {
     E *elem = slot<E>(st, S_ELEM0, M);
     E *elem_alt = slot<E>(st, S_ELEM1, M);
-    Emit e{pord.sa, pord.isa, ph.pid, moff, ph.D, ph.z};
-    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-    device_scan<uint32_t, OpAdd>(st, ph.z, LoadEmitCount{e},
-                                 StoreEmit<E>{e, mb, mc, dT, n, W, elem, M, st->d_flags}, false,
-                                 (uint32_t *)st->d_scalars);
+    const uint32_t z = ph.z;
+    Emit e{pord.sa, pord.isa, ph.pid, moff, ph.D, z};
+    uint32_t *emq = slot<uint32_t>(st, S_TMP0, z);
+    uint32_t *ecnt = slot<uint32_t>(st, S_TMP1, (size_t)z + 1);
+    uint8_t *emp = (uint8_t *)slot<uint32_t>(st, S_TMP2, z / 4 + 1);
+    k_emit_prep<<<grid_for(z, 256), 256, 0, st->stream>>>(e, ph.pidpc, dT, n, W, emq, emp, ecnt);
+    after_launch(st);
+    // in-place exclusive scan of the counts; ecnt[z] = total
+    device_scan<uint32_t, OpAdd>(st, z, LoadArr<uint32_t>{ecnt}, StoreArr<uint32_t>{ecnt}, false, ecnt + z);
+    k_emit<E><<<grid_for(z, EM_T), EM_T, 0, st->stream>>>(z, ecnt, emq, emp, moff, mb, mc, elem, M, st->d_flags);
+    after_launch(st);
     uint32_t *nv = nullptr, *nv2 = nullptr;
     radix_sort<E, false>(st, elem, elem_alt, nv, nv2, M, 8, 8 + bits_for(B - 1));
     probe_begin(st, GBWT_PROBE_MIXED_SCATTER);
-    k_mixed_scatter<E><<<grid_for(M, 256), 256, 0, st->stream>>>(elem, M, delta, B, dOut, n, st->d_flags);
+    k_mixed_scatter<E><<<grid_for((M + 3) / 4, 256), 256, 0, st->stream>>>(elem, M, delta, B, dOut, n, st->d_flags);
     probe_end(st, GBWT_PROBE_MIXED_SCATTER, (uint64_t)M * (sizeof(E) + 1));
     after_launch(st);
 }
@@ -354,8 +404,11 @@ void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph
     k_primary_index<<<grid_for(ph.z, 256), 256, 0, st->stream>>>(
         PrimaryArgs{ph.pid, pord.isa, ph.doff, ph.dlen, grp_of, goff, ph.z, st->d_flags + 2});
     after_launch(st);
+    uint32_t *tile_first = slot<uint32_t>(st, S_TILEG, grid_for(n, RF_TILE) + 1);
+    k_tile_first<<<grid_for(G, 256), 256, 0, st->stream>>>(goff, G, tile_first);
+    after_launch(st);
     probe_begin(st, GBWT_PROBE_RUN_FILL);
-    k_run_fill<<<grid_for(n, RF_TILE), RF_THREADS, 0, st->stream>>>(dOut, n, goff, G, gchar, gmix);
+    k_run_fill<<<grid_for(n, RF_TILE), RF_THREADS, 0, st->stream>>>(dOut, n, goff, G, gchar, gmix, tile_first);
     probe_end(st, GBWT_PROBE_RUN_FILL, (uint64_t)n + 7ull * G);
     after_launch(st);
     stage_mark(st, 5);

@@ -8,10 +8,12 @@
 // occurrence is fingerprinted (polynomial hash mod 2^61-1 over a CTA-staged
 // text window), inserted into an open-addressing table sized to stay in L2
 // when the dictionary is small, and then compared byte for byte with its
-// table representative (the smallest occurrence index), so ids are exact.
-// A fingerprint collision or table overflow is detected on the device and
-// the stage is re-run with a new seed or a larger table.  Dense ids follow
-// first occurrence, which makes the result deterministic.
+// table representative (the occurrence that inserted the key), so ids are
+// exact.  A fingerprint collision or table overflow is detected on the
+// device and the stage is re-run with a new seed or a larger table.  Which
+// occurrence wins an insert varies from run to run, so internal ids may too;
+// nothing downstream depends on them (phrase order comes from the
+// dictionary sort), and every output is deterministic.
 #include "prims.cuh"
 
 namespace gbwt {
@@ -58,7 +60,8 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     const uint32_t sa = k0 ? a.D[k0 - 1] - (uint32_t)a.W + 1u : 0u;
     const uint32_t sb = a.D[klast];
     const uint32_t a_al = sa & ~15u;
-    const bool staged = (size_t)(sb - a_al) + 16 <= PH_SPAN;
+    // +32: the word reads of the last chunk may touch 8 bytes past the span
+    const bool staged = (size_t)(sb - a_al) + 32 <= PH_SPAN;
     if (staged) {
         const bool aligned = (((uintptr_t)a.T) & 15u) == 0;
         const uint32_t nvec = (sb - a_al) / 16 + 1;
@@ -81,19 +84,26 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     if (k >= a.z) return;
     uint32_t start, end;
     phrase_span(a.D, k, a.W, start, end);
+    const uint32_t len = end - start + 1u;
+    // polynomial over little-endian 4-byte chunks (the last one zero-padded)
     uint64_t h = 0;
     if (staged) {
-        for (uint32_t p = start; p <= end; p++) {
-            h = mulmod61(h, a.base) + s_txt[p - a_al] + 1u;
+        const uint32_t *w = (const uint32_t *)s_txt;
+        for (uint32_t i = 0; i < len; i += 4) {
+            const uint32_t p = start - a_al + i;
+            uint32_t chunk = __funnelshift_r(w[p >> 2], w[(p >> 2) + 1], (p & 3u) * 8u);
+            if (len - i < 4) chunk &= (1u << (8u * (len - i))) - 1u;
+            h = mulmod61(h, a.base) + chunk + 1u;
             if (h >= M61) h -= M61;
         }
     } else {
-        for (uint32_t p = start; p <= end; p++) {
-            h = mulmod61(h, a.base) + text_at(a.T, a.n, p) + 1u;
+        for (uint32_t i = 0; i < len; i += 4) {
+            uint32_t chunk = 0;
+            for (uint32_t b = 0; b < 4 && i + b < len; b++) chunk |= (uint32_t)text_at(a.T, a.n, start + i + b) << (8 * b);
+            h = mulmod61(h, a.base) + chunk + 1u;
             if (h >= M61) h -= M61;
         }
     }
-    const uint32_t len = end - start + 1u;
     uint64_t key = h ^ ((uint64_t)len * 0x9E3779B97F4A7C15ull);
     if (key == 0) key = 1;
     uint32_t pos = (uint32_t)((key * 0xD6E8FEB86659FD93ull) >> (64 - a.logc));
@@ -101,6 +111,8 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     for (uint32_t probe = 0; probe <= a.cmask; probe++) {
         unsigned long long cur = atomicCAS(a.tkeys + pos, 0ull, (unsigned long long)key);
         if (cur == 0ull) {
+            // the inserting occurrence is the slot's representative
+            a.tvals[pos] = k;
             uint32_t c = atomicAdd(a.flags + 1, 1u);
             if (c >= a.limit) atomicOr(a.flags, ERR_TABLE_FULL);
             ok = true;
@@ -115,7 +127,6 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
         a.slot_of[k] = 0;
         return;
     }
-    atomicMin(a.tvals + pos, k);
     a.slot_of[k] = pos;
 }
 
@@ -166,8 +177,8 @@ struct StoreDense {
 // pid per occurrence; occurrence counts and the min/max preceding byte of
 // every distinct phrase (warp-aggregated over equal ids).
 __global__ void k_phrase_finalize(const uint8_t *T, uint32_t n, const uint32_t *D, uint32_t z, int W,
-                                  const uint32_t *slot_of, const uint32_t *tdense, uint32_t *pid, uint32_t *occ,
-                                  uint32_t *pcmin, uint32_t *pcmax)
+                                  const uint32_t *slot_of, const uint32_t *tdense, uint32_t *pid, uint32_t *pidpc,
+                                  uint32_t *occ, uint32_t *pcmin, uint32_t *pcmax)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = k < z;
@@ -178,6 +189,7 @@ __global__ void k_phrase_finalize(const uint8_t *T, uint32_t n, const uint32_t *
         uint32_t s, e;
         phrase_span(D, k, W, s, e);
         c = preceding_byte(T, n, s);
+        if (pidpc) pidpc[k] = (id << 8) | c;     // only when ids fit 24 bits
     }
     const unsigned peers = __match_any_sync(0xFFFFFFFFu, id);
     const uint32_t cmin = __reduce_min_sync(peers, c);
@@ -239,7 +251,6 @@ void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph)
         dlen = slot<uint32_t>(st, S_DLEN, (size_t)z + 1);
         dstart = slot<uint32_t>(st, S_DSTART, (size_t)z + 1);
         check_cuda(cudaMemsetAsync(tkeys, 0, (size_t)c * 8, st->stream));
-        check_cuda(cudaMemsetAsync(tvals, 0xFF, (size_t)c * 4, st->stream));
         check_cuda(cudaMemsetAsync(st->d_flags, 0, 8, st->stream));
         check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
         HashArgs a;
@@ -281,8 +292,10 @@ void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph)
     check_cuda(cudaMemsetAsync(occ, 0, (size_t)d * 4, st->stream));
     check_cuda(cudaMemsetAsync(pcmin, 0xFF, (size_t)d * 4, st->stream));
     check_cuda(cudaMemsetAsync(pcmax, 0, (size_t)d * 4, st->stream));
-    k_phrase_finalize<<<grid_for(z, 256), 256, 0, st->stream>>>(dT, n, ph.D, z, W, slot_of, tdense, pid, occ,
-                                                                pcmin, pcmax);
+    uint32_t *pidpc = d < (1u << 24) ? slot<uint32_t>(st, S_PIDPC, z) : nullptr;
+    k_phrase_finalize<<<grid_for(z, 256), 256, 0, st->stream>>>(dT, n, ph.D, z, W, slot_of, tdense, pid, pidpc,
+                                                                occ, pcmin, pcmax);
+    ph.pidpc = pidpc;
     after_launch(st);
     // dictionary offsets (64-bit scan, checked against 2^32)
     uint32_t *doff = slot<uint32_t>(st, S_DOFF, (size_t)d + 1);

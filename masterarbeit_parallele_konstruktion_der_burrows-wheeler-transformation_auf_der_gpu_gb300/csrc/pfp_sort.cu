@@ -22,6 +22,8 @@
 // sorted with the project's stable LSD radix sort; group starts and new heads
 // come from one component-wise max-scan.
 #include "prims.cuh"
+#include <stdio.h>
+#include <stdlib.h>
 
 namespace gbwt {
 
@@ -162,6 +164,284 @@ struct StoreActiveR {
     }
 };
 
+// ---------------------------------------------------------------------
+// Segmented round for small groups.  After the first rounds almost every
+// group is small (a repetitive text's copies of one position), so a CTA
+// sorts whole groups in shared memory instead of running global radix
+// passes.  CTA b owns the groups that start in active indices
+// [b*SS_TILE, (b+1)*SS_TILE); a group may run past the tile by at most
+// SS_SEGMAX elements, so a CTA holds < SS_TILE + SS_SEGMAX elements.
+// ---------------------------------------------------------------------
+constexpr int SS_THREADS = 512;
+constexpr int SS_TILE = 2048;
+constexpr int SS_SEGMAX = 2048;
+constexpr int SS_CAP = SS_TILE + SS_SEGMAX;
+constexpr int SS_PER_THREAD = SS_CAP / SS_THREADS;
+constexpr uint32_t SS_WARPMAX = 256;      // larger groups are sorted by the CTA
+constexpr uint32_t SS_COUNTMAX = 12;      // smaller groups rank by counting, unsorted
+constexpr int SS_MISC_WORDS = 4 + 64 + 16; // misc, scan scratch (32 x u64), big-group list
+constexpr size_t SS_SMEM = (size_t)SS_CAP * (8 + 4 + 4 + 4 + 2) + SS_MISC_WORDS * 4;
+
+// Sorts key[0..s) ascending with a bitonic network whose merge steps start
+// with the "flipped" comparator (i, block_end-1-i): every comparator is
+// ascending, so the virtual padding to a power of two (positions >= s, seen
+// as +infinity) never moves and needs no storage.  Run by `nthr` threads
+// (a warp, or the whole CTA when `cta`).
+__device__ __forceinline__ void bitonic_flip_sort(uint64_t *key, uint32_t s, uint32_t tid, uint32_t nthr, bool cta)
+{
+    if (s < 2) return;
+    uint32_t lgh = 0;                       // log2(k/2)
+    for (uint32_t k = 2; (k >> 1) < s; k <<= 1, lgh++) {
+        for (uint32_t p = tid; p < (s + 1) / 2 + k / 2; p += nthr) {
+            const uint32_t blk = p >> lgh, r = p & ((k >> 1) - 1);
+            const uint32_t i = blk * k + r, l = blk * k + k - 1 - r;
+            if (l < s) {
+                const uint64_t a = key[i], b = key[l];
+                if (a > b) { key[i] = b; key[l] = a; }
+            }
+        }
+        if (cta) __syncthreads(); else __syncwarp();
+        for (uint32_t jj = k >> 2; jj > 0; jj >>= 1) {
+            for (uint32_t p = tid; p < (s + 1) / 2 + jj; p += nthr) {
+                const uint32_t i = 2 * p - (p & (jj - 1)), l = i + jj;
+                if (l < s) {
+                    const uint64_t a = key[i], b = key[l];
+                    if (a > b) { key[i] = b; key[l] = a; }
+                }
+            }
+            if (cta) __syncthreads(); else __syncwarp();
+        }
+    }
+}
+
+// Warp sort of key[0..s), s <= 32*E, in registers: E keys per lane in
+// blocked order (element lane*E+e), +infinity padding, bitonic network with
+// in-lane compare-exchanges for distances < E and shfl_xor across lanes for
+// the others.
+template <int E>
+__device__ __forceinline__ void warp_sort_regs(uint64_t *key, uint32_t s, uint32_t lane)
+{
+    constexpr uint32_t N = 32u * E;
+    uint64_t v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const uint32_t i = lane * E + e;
+        v[e] = i < s ? key[i] : ~0ull;
+    }
+#pragma unroll
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= (uint32_t)E) {
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const uint32_t i = lane * E + e;
+                    const uint64_t o = __shfl_xor_sync(0xFFFFFFFFu, v[e], j / E);
+                    const bool asc = (i & k) == 0, lower = (i & j) == 0;
+                    v[e] = (lower == asc) ? (v[e] < o ? v[e] : o) : (v[e] > o ? v[e] : o);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    if ((e & j) == 0) {
+                        const int e2 = e | (int)j;
+                        const uint32_t i = lane * E + e;
+                        const bool asc = (i & k) == 0;
+                        if ((v[e] > v[e2]) == asc) { const uint64_t t = v[e]; v[e] = v[e2]; v[e2] = t; }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const uint32_t i = lane * E + e;
+        if (i < s) key[i] = v[e];
+    }
+    __syncwarp();
+}
+
+// key2[a] = isa[x+h] + 1 for every active element (all reads of this round's
+// ranks happen before any update); flags[3] counts groups too large for the
+// shared-memory path.
+__global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
+                               uint32_t h, uint32_t *key2, uint32_t *flags)
+{
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    key2[a] = isa[act_x[a] + h] + 1u;
+    const uint32_t g = act_g[a];
+    const bool gnew = a == 0 || act_g[a - 1] != g;
+    if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
+}
+
+template <typename Rem>
+__global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restrict__ act_x,
+                                                         const uint32_t *__restrict__ act_g,
+                                                         const uint32_t *__restrict__ key2, uint32_t A, uint32_t h2,
+                                                         Rem rem, uint32_t *isa, uint32_t *sa, uint32_t *out_x,
+                                                         uint32_t *out_g, uint8_t *out_flag, uint32_t *flags)
+{
+    extern __shared__ __align__(16) unsigned char ss_smem[];
+    uint64_t *s_key = (uint64_t *)ss_smem;
+    uint32_t *s_x = (uint32_t *)(s_key + SS_CAP);
+    uint32_t *s_sg = s_x + SS_CAP;       // segment -> group head g
+    uint32_t *s_ss = s_sg + SS_CAP;      // segment -> local start index
+    uint32_t *s_misc = s_ss + SS_CAP;    // [0] first start, [1] end, [2] warp counter, [3] big groups
+    uint64_t *s_scan = (uint64_t *)(s_misc + 4);
+    uint16_t *s_seg = (uint16_t *)(s_misc + SS_MISC_WORDS);   // element -> segment
+
+    const uint32_t a_lo = blockIdx.x * SS_TILE;
+    const uint32_t a_hi = min(a_lo + (uint32_t)SS_TILE, A);
+    if (threadIdx.x == 0) { s_misc[0] = 0xFFFFFFFFu; s_misc[1] = 0xFFFFFFFFu; }
+    __syncthreads();
+    for (uint32_t a = a_lo + threadIdx.x; a < a_hi; a += SS_THREADS)
+        if (a == 0 || act_g[a - 1] != act_g[a]) atomicMin(&s_misc[0], a);
+    const uint32_t e_lim = min(a_hi + (uint32_t)SS_SEGMAX, A);
+    for (uint32_t a = a_hi + threadIdx.x; a < e_lim; a += SS_THREADS)
+        if (act_g[a - 1] != act_g[a]) atomicMin(&s_misc[1], a);
+    __syncthreads();
+    const uint32_t s0 = s_misc[0];
+    if (s0 == 0xFFFFFFFFu) return;                   // no group starts in this tile
+    uint32_t e1 = s_misc[1];
+    if (e1 == 0xFFFFFFFFu) {
+        if (e_lim < A) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
+        e1 = A;
+    }
+    const uint32_t cnt = e1 - s0;
+
+    // blocked load: thread t owns local indices [t*SS_PER_THREAD, +SS_PER_THREAD)
+    const uint32_t i0 = threadIdx.x * SS_PER_THREAD;
+    uint32_t nseg = 0;
+    bool gn[SS_PER_THREAD];
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t i = i0 + j;
+        gn[j] = false;
+        if (i < cnt) {
+            const uint32_t a = s0 + i;
+            gn[j] = i == 0 || act_g[a - 1] != act_g[a];
+            nseg += gn[j];
+        }
+    }
+    uint64_t tot;
+    uint32_t seg = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nseg, tot, OpAdd(), s_scan);
+    const uint32_t nsegs = (uint32_t)tot;
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t i = i0 + j;
+        if (i < cnt) {
+            const uint32_t a = s0 + i;
+            if (gn[j]) { s_sg[seg] = act_g[a]; s_ss[seg] = i; seg++; }
+            // unique key: (isa[x+h]+1, local index) -- stable, deterministic
+            s_key[i] = ((uint64_t)key2[a] << 32) | i;
+            s_x[i] = act_x[a];
+            s_seg[i] = (uint16_t)(seg - 1);
+        }
+    }
+    if (threadIdx.x == 0) { s_ss[nsegs] = cnt; s_misc[2] = 0; s_misc[3] = 0; }
+    __syncthreads();
+
+    // Tier 3: groups larger than SS_WARPMAX are sorted by the whole CTA.
+    uint32_t *s_big = s_misc + 4 + 64;             // after the scan scratch
+    for (uint32_t sg = threadIdx.x; sg < nsegs; sg += SS_THREADS)
+        if (s_ss[sg + 1] - s_ss[sg] > SS_WARPMAX) s_big[atomicAdd(&s_misc[3], 1u)] = sg;
+    __syncthreads();
+    const uint32_t nbig = s_misc[3];
+    for (uint32_t b = 0; b < nbig; b++) {
+        const uint32_t ss = s_ss[s_big[b]], s = s_ss[s_big[b] + 1] - ss;
+        bitonic_flip_sort(s_key + ss, s, threadIdx.x, SS_THREADS, true);
+    }
+
+    // Tier 1: groups of at most SS_COUNTMAX elements -- every element counts the
+    // smaller keys of its group (no sort at all).
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t i = i0 + j;
+        if (i >= cnt) break;
+        const uint32_t sg = s_seg[i];
+        const uint32_t ss = s_ss[sg], se = s_ss[sg + 1];
+        if (se - ss > SS_COUNTMAX) continue;
+        const uint64_t kk = s_key[i];
+        const uint32_t k2 = (uint32_t)(kk >> 32);
+        uint32_t lt = 0, eqb = 0, eq = 0;
+        for (uint32_t m = ss; m < se; m++) {
+            const uint32_t o = (uint32_t)(s_key[m] >> 32);
+            lt += o < k2;
+            eq += o == k2;
+            eqb += (o == k2) & (m < i);
+        }
+        const uint32_t g = s_sg[sg];
+        const uint32_t x = s_x[i];
+        const bool done = eq == 1 || rem(x) <= h2;
+        const uint32_t nh = g + lt, loc = lt + eqb;
+        isa[x] = nh;
+        if (done) sa[g + loc] = x;
+        out_x[s0 + ss + loc] = x;
+        out_g[s0 + ss + loc] = nh;
+        out_flag[s0 + ss + loc] = done ? 0 : 1;
+    }
+
+    // Tiers 2/3: warps take the larger groups from a shared counter, sort the
+    // ones up to SS_WARPMAX, and derive the new heads of all of them.
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t sg = 0;
+        if (lane == 0) {
+            do {
+                sg = atomicAdd(&s_misc[2], 1u);
+            } while (sg < nsegs && s_ss[sg + 1] - s_ss[sg] <= SS_COUNTMAX);
+        }
+        sg = __shfl_sync(0xFFFFFFFFu, sg, 0);
+        if (sg >= nsegs) break;
+        const uint32_t ss = s_ss[sg], se = s_ss[sg + 1], s = se - ss;
+        const uint32_t g = s_sg[sg];
+        uint64_t *key = s_key + ss;
+        if (s <= 32) warp_sort_regs<1>(key, s, lane);
+        else if (s <= 64) warp_sort_regs<2>(key, s, lane);
+        else if (s <= 128) warp_sort_regs<4>(key, s, lane);
+        else if (s <= SS_WARPMAX) warp_sort_regs<8>(key, s, lane);
+        // new heads: start of each run of equal key2 (carried across chunks)
+        uint32_t carry = 0;
+        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+            const uint32_t i = c0 + lane;
+            const bool in = i < s;
+            const uint64_t kk = in ? key[i] : 0ull;
+            const uint32_t k2 = (uint32_t)(kk >> 32);
+            const bool knew = in && (i == 0 || (uint32_t)(key[i - 1] >> 32) != k2);
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, knew);
+            const unsigned upto = bal & (0xFFFFFFFFu >> (31u - lane));
+            const uint32_t gstart = upto ? c0 + 31u - __clz(upto) : carry;
+            if (in) {
+                const bool single = knew && (i + 1 == s || (uint32_t)(key[i + 1] >> 32) != k2);
+                const uint32_t x = s_x[(uint32_t)kk & 0xFFFFu];
+                const uint32_t nh = g + gstart;
+                const bool done = single || rem(x) <= h2;
+                isa[x] = nh;
+                if (done) sa[g + i] = x;
+                out_x[s0 + ss + i] = x;
+                out_g[s0 + ss + i] = nh;
+                out_flag[s0 + ss + i] = done ? 0 : 1;
+            }
+            const uint32_t last = __shfl_sync(0xFFFFFFFFu, gstart, 31);
+            carry = last;
+        }
+    }
+}
+
+struct LoadFlag8 {
+    const uint8_t *f;
+    __device__ __forceinline__ uint32_t operator()(size_t a) const { return f[a]; }
+};
+struct StoreCompact {
+    const uint32_t *sx, *sg;
+    uint32_t *ax, *ag;
+    __device__ __forceinline__ void operator()(size_t a, uint32_t pre, uint32_t v) const
+    {
+        if (v) { ax[pre] = sx[a]; ag[pre] = sg[a]; }
+    }
+};
+
 // Sorts N positions; key0 (in slot S_KEY0) holds the initial keys covering
 // h0 symbols.  Fills isa[N] and sa[N]; returns the number of rounds.
 template <typename Rem>
@@ -190,8 +470,42 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     const int lb = bits_for(N);          // isa+1 <= N
     const int gb = bits_for(N - 1);
     uint64_t h = h0;
+    static bool ss_attr = false;
+    if (!ss_attr) {
+        check_cuda(cudaFuncSetAttribute(k_seg_sort<Rem>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SS_SMEM));
+        ss_attr = true;
+    }
+    const bool debug = getenv("GBWT_DEBUG") != nullptr;
     while (A > 0) {
         if (h >= N) throw Error{GBWT_INTERNAL_ERROR};
+        const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
+        // gather this round's keys before any rank changes; count big groups
+        uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
+        check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
+        k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
+                                                                 st->d_flags);
+        after_launch(st);
+        check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
+        check_cuda(cudaStreamSynchronize(st->stream));
+        const bool big = ((uint32_t)st->h_scalars[2]) != 0;
+        if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u path=%s\n", (unsigned long long)h, A,
+                           big ? "global" : "segmented");
+        if (!big) {
+            uint32_t *sx = slot<uint32_t>(st, S_KEY1, N);       // key arrays are free here
+            uint32_t *sg = slot<uint32_t>(st, S_VAL1, N);
+            uint8_t *sf = (uint8_t *)slot<uint32_t>(st, S_VAL0, N);
+            k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
+                act_x, act_g, key2, A, h2, rem, isa, sa, sx, sg, sf, st->d_flags);
+            after_launch(st);
+            check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+            device_scan<uint32_t, OpAdd>(st, A, LoadFlag8{sf}, StoreCompact{sx, sg, act_x, act_g}, false,
+                                         (uint32_t *)st->d_scalars);
+            fetch_scalars(st, 1);
+            A = (uint32_t)st->h_scalars[0];
+            h *= 2;
+            rounds++;
+            continue;
+        }
         // the key arrays of the previous round are dead: rebuild in place
         uint64_t *k = slot<uint64_t>(st, S_KEY0, N);
         uint64_t *k_alt = slot<uint64_t>(st, S_KEY1, N);
