@@ -127,6 +127,24 @@ int64_t gbwt_pfp_trigger_scan(void *storage, const uint8_t *T, int64_t n, int32_
 int64_t gbwt_pfp_parse(void *storage, const uint8_t *T, int64_t n, int32_t W, int32_t P,
                        uint32_t flags, int32_t *ranks, int32_t *parse_sa, int64_t capacity);
 
+/*
+ * Trigger scan that allocates nothing.  No counterpart in the reference: it
+ * serves callers that cannot allocate device memory (a host framework that
+ * hands out a fixed budget, an allocator that must not be re-entered, a
+ * process that reserved all device memory up front).  T (n bytes) and D
+ * (capacity uint32 slots) are DEVICE pointers owned by the caller; `stream`
+ * is a cudaStream_t (NULL = legacy default stream).  Writes the phrase end
+ * positions D[0..z) exactly like gbwt_pfp_trigger_scan and returns z after
+ * synchronising the stream.
+ * Limits: n <= 2^30 bytes.  The scratch is one library-wide device array of
+ * about 1 MiB that every GPU loading the library keeps until exit; the first
+ * call on a device looks up its address (do that call before any stream
+ * capture).  Calls that overlap on the GPU race on that array and must be
+ * serialised by the caller; each call clears what must start at zero.
+ */
+int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, int32_t P, uint32_t flags,
+                                      uint32_t *D, int64_t capacity, void *stream);
+
 /* Copies the counts of the last call into *out. */
 int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
 

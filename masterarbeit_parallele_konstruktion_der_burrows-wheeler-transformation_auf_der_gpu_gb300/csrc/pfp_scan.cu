@@ -16,6 +16,7 @@
 // positions are compacted with popc + a CTA scan; the count pass also
 // validates the input bytes (K:130-132) without trapping.
 #include "prims.cuh"
+#include <mutex>
 
 namespace gbwt {
 
@@ -234,4 +235,114 @@ uint32_t run_trigger_scan(Storage *st, const uint8_t *dT, uint32_t n, int W, int
     return (uint32_t)st->h_scalars[0] + 1u;
 }
 
+// ---------------------------------------------------------------------
+// Allocation-free trigger scan.
+//
+// Some callers cannot allocate device memory themselves: code running
+// under a fixed memory budget handed out by a host framework, an allocator
+// that must not be re-entered from a callback, or a process that pins all
+// device memory up front.  For them the trigger scan also runs without a
+// storage object and without any cudaMalloc: its scratch (per-CTA trigger
+// counts, the scan's tile partials, the error/total words) lives in the
+// file-scope array below, which every GPU that loads this library holds
+// until the process exits (NOALLOC_SCRATCH_WORDS * 4 bytes, about 1 MiB).
+// Texts are limited to NOALLOC_MAX_N bytes by that size.  All calls share
+// the array: calls whose work overlaps on the GPU (other streams, other host
+// threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------
+constexpr int64_t NOALLOC_MAX_N = (int64_t)1 << 30;
+constexpr uint32_t NOALLOC_MAX_BLOCKS = (uint32_t)(NOALLOC_MAX_N / TS_TILE);
+constexpr uint32_t NOALLOC_PARTIALS = (NOALLOC_MAX_BLOCKS + SC_TILE - 1) / SC_TILE;
+constexpr uint32_t NOALLOC_SCRATCH_WORDS = NOALLOC_MAX_BLOCKS + 256 + 64;
+
+static __device__ __align__(256) uint32_t g_trigger_scratch[NOALLOC_SCRATCH_WORDS];
+
+// Device address of g_trigger_scratch for the current device, looked up
+// once per device (the host-side symbol itself is not a device address).
+static uint32_t *noalloc_scratch_ptr()
+{
+    static uint32_t *ptrs[64] = {};
+    static std::mutex mu;
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error{GBWT_GPU_NOT_SUPPORTED};
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        check_cuda(cudaGetSymbolAddress(&p, g_trigger_scratch));
+        ptrs[dev] = (uint32_t *)p;
+    }
+    return ptrs[dev];
+}
+
+template <int WT, int PT>
+static int64_t noalloc_launch(const ScanArgs &a, unsigned blocks, uint32_t *scratch, uint32_t *D, int64_t capacity,
+                              cudaStream_t stream)
+{
+    uint32_t *counts = scratch;                         // [NOALLOC_MAX_BLOCKS]
+    uint32_t *partials = scratch + NOALLOC_MAX_BLOCKS;  // [256]
+    uint32_t *words = partials + 256;                   // [0] errors, [1] trigger count
+    check_cuda(cudaMemsetAsync(words, 0, 64 * sizeof(uint32_t), stream));
+    ScanArgs b = a;
+    b.flags = words;
+    k_trigger<WT, PT, false><<<blocks, TS_THREADS, 0, stream>>>(b, counts, nullptr, nullptr);
+    check_cuda(cudaGetLastError());
+    const unsigned tiles = (blocks + SC_TILE - 1) / SC_TILE;
+    if (tiles == 1) {
+        k_scan_down<uint32_t, OpAdd><<<1, SC_THREADS, 0, stream>>>(LoadArr<uint32_t>{counts}, StoreArr<uint32_t>{counts},
+                                                                    blocks, (const uint32_t *)nullptr, false, words + 1);
+    } else {
+        k_scan_reduce<uint32_t, OpAdd><<<tiles, SC_THREADS, 0, stream>>>(LoadArr<uint32_t>{counts}, blocks, partials);
+        k_scan_down<uint32_t, OpAdd><<<1, SC_THREADS, 0, stream>>>(LoadArr<uint32_t>{partials},
+                                                                    StoreArr<uint32_t>{partials}, tiles,
+                                                                    (const uint32_t *)nullptr, false, (uint32_t *)nullptr);
+        k_scan_down<uint32_t, OpAdd><<<tiles, SC_THREADS, 0, stream>>>(LoadArr<uint32_t>{counts},
+                                                                        StoreArr<uint32_t>{counts}, blocks, partials,
+                                                                        false, words + 1);
+    }
+    check_cuda(cudaGetLastError());
+    uint32_t host_words[2] = {0, 0};
+    check_cuda(cudaMemcpyAsync(host_words, words, sizeof(host_words), cudaMemcpyDeviceToHost, stream));
+    check_cuda(cudaStreamSynchronize(stream));
+    if (host_words[0] & ERR_BAD_BYTE) return GBWT_BAD_PARAMETER;
+    if (host_words[0] & ERR_SMALL_RANGE) return GBWT_UNSUPPORTED_INPUT;
+    const uint32_t c = host_words[1];
+    if ((int64_t)c + 1 > capacity) return GBWT_BAD_PARAMETER;
+    k_trigger<WT, PT, true><<<blocks, TS_THREADS, 0, stream>>>(b, nullptr, counts, D);
+    k_set_u32<<<1, 1, 0, stream>>>(D + c, a.n + (uint32_t)a.W - 1u);
+    check_cuda(cudaGetLastError());
+    check_cuda(cudaStreamSynchronize(stream));
+    return (int64_t)c + 1;
+}
+
 }  // namespace gbwt
+
+extern "C" int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, int32_t P, uint32_t flags,
+                                                 uint32_t *D, int64_t capacity, void *stream)
+{
+    using namespace gbwt;
+    if (n < 0 || n > NOALLOC_MAX_N || W < 1 || W > 64 || P < 1 || P > 65535) return GBWT_BAD_PARAMETER;
+    if (n == 0) return 0;
+    if (!T || !D || capacity < 1) return GBWT_BAD_PARAMETER;
+    try {
+        uint32_t *scratch = noalloc_scratch_ptr();
+        ScanArgs a;
+        a.T = T; a.n = (uint32_t)n; a.W = W; a.P = P;
+        uint32_t wW = 1;
+        for (int i = 0; i < W; i++) wW = (wW * 2u) % (uint32_t)P;
+        a.wW = wW;
+        a.hi = (flags & GBWT_FLAG_SMALL_ALPHABET) ? 15u : 254u;
+        a.flags = nullptr;
+        const unsigned blocks = grid_for((size_t)n, TS_TILE);
+        cudaStream_t s = (cudaStream_t)stream;
+        if (W == 5 && P == 16) return noalloc_launch<5, 16>(a, blocks, scratch, D, capacity, s);
+        if (W == 5 && P == 11) return noalloc_launch<5, 11>(a, blocks, scratch, D, capacity, s);
+        if (W == 5 && P == 13) return noalloc_launch<5, 13>(a, blocks, scratch, D, capacity, s);
+        if (W == 5 && P == 14) return noalloc_launch<5, 14>(a, blocks, scratch, D, capacity, s);
+        if (W == 5 && P == 23) return noalloc_launch<5, 23>(a, blocks, scratch, D, capacity, s);
+        if (W == 35 && P == 81) return noalloc_launch<35, 81>(a, blocks, scratch, D, capacity, s);
+        return noalloc_launch<0, 0>(a, blocks, scratch, D, capacity, s);
+    } catch (const Error &e) {
+        return e.code;
+    }
+}
