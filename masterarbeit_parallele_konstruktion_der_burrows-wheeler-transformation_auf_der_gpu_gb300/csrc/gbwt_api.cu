@@ -137,6 +137,7 @@ static int64_t pipeline(Storage *st, const uint8_t *T, uint8_t *L, int64_t n, in
     check_cuda(cudaStreamSynchronize(st->stream));
     uint32_t hflags[4];
     memcpy(hflags, st->h_scalars + 8, sizeof(hflags));
+    if (hflags[0] & ERR_TIMEOUT) return GBWT_TIMEOUT;
     if (hflags[0] & ERR_INTERNAL) return GBWT_INTERNAL_ERROR;
     st->stats.primary_index = hflags[2];
     harvest_probe(st);

@@ -18,6 +18,7 @@ enum : uint32_t {
     ERR_COLLISION    = 1u << 2,   // two different phrases share a fingerprint
     ERR_TABLE_FULL   = 1u << 3,   // phrase table exceeded its load limit
     ERR_INTERNAL     = 1u << 4,   // an internal consistency check failed
+    ERR_TIMEOUT      = 1u << 5,   // a bounded device wait gave up
 };
 
 // Scratch slots; each grows on demand and is reused by later calls.
@@ -30,7 +31,7 @@ enum Slot : int {
     S_GCOUNT, S_GCHAR, S_GMIX, S_GOFF, S_GRP, S_MOFF, S_MB, S_MC, S_MIXIDX, S_DELTA,
     S_ELEM0, S_ELEM1,
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
-    S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG,
+    S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2,
     S_NUM
 };
 

@@ -179,8 +179,10 @@ constexpr int SS_CAP = SS_TILE + SS_SEGMAX;
 constexpr int SS_PER_THREAD = SS_CAP / SS_THREADS;
 constexpr uint32_t SS_WARPMAX = 256;      // larger groups are sorted by the CTA
 constexpr uint32_t SS_COUNTMAX = 12;      // smaller groups rank by counting, unsorted
-constexpr int SS_MISC_WORDS = 4 + 64 + 16; // misc, scan scratch (32 x u64), big-group list
-constexpr size_t SS_SMEM = (size_t)SS_CAP * (8 + 4 + 4 + 4 + 2) + SS_MISC_WORDS * 4;
+constexpr int SS_MISC_WORDS = 8 + 64 + 16; // misc, scan scratch (32 x u64), big-group list
+// keys, x, segment heads, segment starts, slot heads (4 B each), misc,
+// element -> segment and slot -> element (2 B each)
+constexpr size_t SS_SMEM = (size_t)SS_CAP * (8 + 4 + 4 + 4 + 4 + 2 + 2) + SS_MISC_WORDS * 4;
 
 // Sorts key[0..s) ascending with a bitonic network whose merge steps start
 // with the "flipped" comparator (i, block_end-1-i): every comparator is
@@ -276,20 +278,23 @@ __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, con
 }
 
 template <typename Rem>
-__global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restrict__ act_x,
-                                                         const uint32_t *__restrict__ act_g,
-                                                         const uint32_t *__restrict__ key2, uint32_t A, uint32_t h2,
-                                                         Rem rem, uint32_t *isa, uint32_t *sa, uint32_t *out_x,
-                                                         uint32_t *out_g, uint8_t *out_flag, uint32_t *flags)
+__global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__restrict__ act_x,
+                                                            const uint32_t *__restrict__ act_g,
+                                                            const uint32_t *__restrict__ key2, uint32_t A, uint32_t h2,
+                                                            Rem rem, uint32_t *isa, uint32_t *sa, uint32_t *out_x,
+                                                            uint32_t *out_g, uint32_t *counter, uint32_t *flags)
 {
     extern __shared__ __align__(16) unsigned char ss_smem[];
-    uint64_t *s_key = (uint64_t *)ss_smem;
-    uint32_t *s_x = (uint32_t *)(s_key + SS_CAP);
-    uint32_t *s_sg = s_x + SS_CAP;       // segment -> group head g
-    uint32_t *s_ss = s_sg + SS_CAP;      // segment -> local start index
-    uint32_t *s_misc = s_ss + SS_CAP;    // [0] first start, [1] end, [2] warp counter, [3] big groups
-    uint64_t *s_scan = (uint64_t *)(s_misc + 4);
-    uint16_t *s_seg = (uint16_t *)(s_misc + SS_MISC_WORDS);   // element -> segment
+    uint64_t *s_key = (uint64_t *)ss_smem;           // (isa[x+h]+1) << 32 | local index
+    uint32_t *s_x = (uint32_t *)(s_key + SS_CAP);    // local index -> x
+    uint32_t *s_sg = s_x + SS_CAP;                   // segment -> group head g
+    uint32_t *s_ss = s_sg + SS_CAP;                  // segment -> local start index
+    uint32_t *s_nh = s_ss + SS_CAP;                  // sorted slot -> new head | done bit
+    uint32_t *s_misc = s_nh + SS_CAP;                // [0] first start, [1] end, [2] warp counter, [3] big, [4] base
+    uint64_t *s_scan = (uint64_t *)(s_misc + 8);
+    uint32_t *s_big = s_misc + 8 + 64;
+    uint16_t *s_seg = (uint16_t *)(s_misc + SS_MISC_WORDS);   // local index -> segment
+    uint16_t *s_perm = s_seg + SS_CAP;                        // sorted slot -> local index
 
     const uint32_t a_lo = blockIdx.x * SS_TILE;
     const uint32_t a_hi = min(a_lo + (uint32_t)SS_TILE, A);
@@ -343,7 +348,6 @@ __global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restr
     __syncthreads();
 
     // Tier 3: groups larger than SS_WARPMAX are sorted by the whole CTA.
-    uint32_t *s_big = s_misc + 4 + 64;             // after the scan scratch
     for (uint32_t sg = threadIdx.x; sg < nsegs; sg += SS_THREADS)
         if (s_ss[sg + 1] - s_ss[sg] > SS_WARPMAX) s_big[atomicAdd(&s_misc[3], 1u)] = sg;
     __syncthreads();
@@ -353,8 +357,8 @@ __global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restr
         bitonic_flip_sort(s_key + ss, s, threadIdx.x, SS_THREADS, true);
     }
 
-    // Tier 1: groups of at most SS_COUNTMAX elements -- every element counts the
-    // smaller keys of its group (no sort at all).
+    // Tier 1: groups of at most SS_COUNTMAX elements -- every element counts
+    // the smaller keys of its group (no sort at all) and records its slot.
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
         const uint32_t i = i0 + j;
@@ -364,22 +368,17 @@ __global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restr
         if (se - ss > SS_COUNTMAX) continue;
         const uint64_t kk = s_key[i];
         const uint32_t k2 = (uint32_t)(kk >> 32);
-        uint32_t lt = 0, eqb = 0, eq = 0;
+        uint32_t lt = 0, eq = 0, pos = 0;
         for (uint32_t m = ss; m < se; m++) {
-            const uint32_t o = (uint32_t)(s_key[m] >> 32);
-            lt += o < k2;
-            eq += o == k2;
-            eqb += (o == k2) & (m < i);
+            const uint64_t o = s_key[m];
+            const uint32_t o2 = (uint32_t)(o >> 32);
+            lt += o2 < k2;
+            eq += o2 == k2;
+            pos += o < kk;
         }
-        const uint32_t g = s_sg[sg];
-        const uint32_t x = s_x[i];
-        const bool done = eq == 1 || rem(x) <= h2;
-        const uint32_t nh = g + lt, loc = lt + eqb;
-        isa[x] = nh;
-        if (done) sa[g + loc] = x;
-        out_x[s0 + ss + loc] = x;
-        out_g[s0 + ss + loc] = nh;
-        out_flag[s0 + ss + loc] = done ? 0 : 1;
+        const bool done = eq == 1 || rem(s_x[i]) <= h2;
+        s_nh[ss + pos] = (s_sg[sg] + lt) | (done ? 0x80000000u : 0u);
+        s_perm[ss + pos] = (uint16_t)i;
     }
 
     // Tiers 2/3: warps take the larger groups from a shared counter, sort the
@@ -414,33 +413,48 @@ __global__ void __launch_bounds__(SS_THREADS) k_seg_sort(const uint32_t *__restr
             const uint32_t gstart = upto ? c0 + 31u - __clz(upto) : carry;
             if (in) {
                 const bool single = knew && (i + 1 == s || (uint32_t)(key[i + 1] >> 32) != k2);
-                const uint32_t x = s_x[(uint32_t)kk & 0xFFFFu];
-                const uint32_t nh = g + gstart;
-                const bool done = single || rem(x) <= h2;
-                isa[x] = nh;
-                if (done) sa[g + i] = x;
-                out_x[s0 + ss + i] = x;
-                out_g[s0 + ss + i] = nh;
-                out_flag[s0 + ss + i] = done ? 0 : 1;
+                const uint32_t li = (uint32_t)kk & 0xFFFFu;
+                const bool done = single || rem(s_x[li]) <= h2;
+                s_nh[ss + i] = (g + gstart) | (done ? 0x80000000u : 0u);
+                s_perm[ss + i] = (uint16_t)li;
             }
-            const uint32_t last = __shfl_sync(0xFFFFFFFFu, gstart, 31);
-            carry = last;
+            carry = __shfl_sync(0xFFFFFFFFu, gstart, 31);
+        }
+    }
+    __syncthreads();
+
+    // Final pass over sorted slots: ranks, finished suffixes, and the CTA's
+    // share of the next active list (reserved with one atomic; the order of
+    // groups in that list does not matter, only each group being contiguous).
+    uint32_t nact = 0;
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t p = i0 + j;
+        if (p < cnt) nact += (s_nh[p] >> 31) ^ 1u;
+    }
+    uint64_t atot;
+    uint32_t apre = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nact, atot, OpAdd(), s_scan);
+    if (threadIdx.x == 0) s_misc[4] = atot ? atomicAdd(counter, (uint32_t)atot) : 0u;
+    __syncthreads();
+    const uint32_t base = s_misc[4];
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t p = i0 + j;
+        if (p >= cnt) break;
+        const uint32_t v = s_nh[p];
+        const uint32_t nh = v & 0x7FFFFFFFu;
+        const uint32_t x = s_x[s_perm[p]];
+        isa[x] = nh;
+        if (v >> 31) {
+            const uint32_t sg = s_seg[p];
+            sa[s_sg[sg] + (p - s_ss[sg])] = x;
+        } else {
+            out_x[base + apre] = x;
+            out_g[base + apre] = nh;
+            apre++;
         }
     }
 }
-
-struct LoadFlag8 {
-    const uint8_t *f;
-    __device__ __forceinline__ uint32_t operator()(size_t a) const { return f[a]; }
-};
-struct StoreCompact {
-    const uint32_t *sx, *sg;
-    uint32_t *ax, *ag;
-    __device__ __forceinline__ void operator()(size_t a, uint32_t pre, uint32_t v) const
-    {
-        if (v) { ax[pre] = sx[a]; ag[pre] = sg[a]; }
-    }
-};
 
 // Sorts N positions; key0 (in slot S_KEY0) holds the initial keys covering
 // h0 symbols.  Fills isa[N] and sa[N]; returns the number of rounds.
@@ -454,6 +468,8 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     uint32_t *vals_alt = slot<uint32_t>(st, S_VAL1, N);
     uint32_t *act_x = slot<uint32_t>(st, S_ACTX, N);
     uint32_t *act_g = slot<uint32_t>(st, S_ACTG, N);
+    uint32_t *act_x2 = slot<uint32_t>(st, S_ACTX2, N);   // next active list (segmented rounds)
+    uint32_t *act_g2 = slot<uint32_t>(st, S_ACTG2, N);
     uint32_t *head = slot<uint32_t>(st, S_HEAD, N);
     int rounds = 1;
 
@@ -491,17 +507,15 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u path=%s\n", (unsigned long long)h, A,
                            big ? "global" : "segmented");
         if (!big) {
-            uint32_t *sx = slot<uint32_t>(st, S_KEY1, N);       // key arrays are free here
-            uint32_t *sg = slot<uint32_t>(st, S_VAL1, N);
-            uint8_t *sf = (uint8_t *)slot<uint32_t>(st, S_VAL0, N);
-            k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
-                act_x, act_g, key2, A, h2, rem, isa, sa, sx, sg, sf, st->d_flags);
-            after_launch(st);
+            uint32_t *counter = (uint32_t *)st->d_scalars;
             check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-            device_scan<uint32_t, OpAdd>(st, A, LoadFlag8{sf}, StoreCompact{sx, sg, act_x, act_g}, false,
-                                         (uint32_t *)st->d_scalars);
+            k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
+                act_x, act_g, key2, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags);
+            after_launch(st);
             fetch_scalars(st, 1);
             A = (uint32_t)st->h_scalars[0];
+            uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
+            uint32_t *t2 = act_g; act_g = act_g2; act_g2 = t2;
             h *= 2;
             rounds++;
             continue;
