@@ -542,29 +542,42 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     return rounds;
 }
 
-// Initial dictionary keys: the next h0 = 7 bytes (or 15 four-bit symbols with
-// the small alphabet) of the phrase suffix, zero past the phrase end, then one
-// bit "the suffix continues past h0".  The bit keeps every group uniform in
-// whether its strings end within h0 symbols: without it a suffix of exactly
-// h0 symbols would tie with longer suffixes sharing those symbols.
-constexpr uint32_t DICT_H0 = 7, DICT_H0_SMALL = 15;
-
-__global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, bool small, uint64_t *keys)
+// Byte values present in the dictionary (= the text's alphabet plus the
+// sentinel byte 1), as a 256-bit set OR-ed into bits[0..8).
+__global__ void k_alpha_present(const uint8_t *dict, uint32_t N, uint32_t *bits)
 {
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < N; x += gridDim.x * blockDim.x) {
+        const uint32_t c = dict[x];
+#pragma unroll
+        for (int w = 0; w < 8; w++) m[w] |= ((c >> 5) == (uint32_t)w) ? (1u << (c & 31u)) : 0u;
+    }
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+        const uint32_t v = __reduce_or_sync(0xFFFFFFFFu, m[w]);
+        if ((threadIdx.x & 31u) == 0 && v) atomicOr(bits + w, v);
+    }
+}
+
+// Initial dictionary keys: the next h0 symbols of the phrase suffix, each
+// recoded to its rank in the alphabet (code 0 = past the phrase end, `bps`
+// bits per symbol, h0 = floor(63 / bps): 21 symbols for DNA, 7 for a full
+// byte alphabet), then one bit "the suffix continues past h0".  The bit keeps
+// every group uniform in whether its strings end within h0 symbols: without
+// it a suffix of exactly h0 symbols would tie with longer suffixes sharing
+// those symbols.  The recoding is monotone, so the order is the byte order.
+__global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, const uint8_t *code, int bps, int h0,
+                            uint64_t *keys)
+{
+    __shared__ uint8_t s_code[256];
+    s_code[threadIdx.x] = code[threadIdx.x];     // blockDim == 256
+    __syncthreads();
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= N) return;
     const uint32_t r = rem(x);
     uint64_t key = 0;
-    if (small) {
-#pragma unroll
-        for (int i = 0; i < (int)DICT_H0_SMALL; i++)
-            key = (key << 4) | (uint64_t)((uint32_t)i < r ? (dict[x + i] & 15u) : 0u);
-        key = (key << 1) | (r > DICT_H0_SMALL ? 1u : 0u);
-    } else {
-#pragma unroll
-        for (int i = 0; i < (int)DICT_H0; i++) key = (key << 8) | (uint64_t)((uint32_t)i < r ? dict[x + i] : 0u);
-        key = (key << 1) | (r > DICT_H0 ? 1u : 0u);
-    }
+    for (int i = 0; i < h0; i++) key = (key << bps) | (uint64_t)((uint32_t)i < r ? s_code[dict[x + i]] : 0u);
+    key = (key << 1) | (r > (uint32_t)h0 ? 1u : 0u);
     keys[x] = key;
 }
 
@@ -591,14 +604,36 @@ struct StoreLexRank {
 void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
 {
     (void)W;
+    (void)small;   // the alphabet recoding below covers the small-alphabet packing
     const uint32_t N = (uint32_t)ph.dict_bytes;
     DictRem rem{ph.dphr, ph.doff, ph.dlen};
+    // alphabet of the dictionary -> dense codes 1..sigma
+    check_cuda(cudaMemsetAsync(st->d_flags + 8, 0, 8 * sizeof(uint32_t), st->stream));
+    unsigned ag = grid_for(N, 256);
+    if (ag > (unsigned)st->num_sms * 4) ag = (unsigned)st->num_sms * 4;
+    k_alpha_present<<<ag, 256, 0, st->stream>>>(ph.dict, N, st->d_flags + 8);
+    after_launch(st);
+    uint32_t present[8];
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 4, st->d_flags + 8, sizeof(present), cudaMemcpyDeviceToHost,
+                               st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    memcpy(present, st->h_scalars + 4, sizeof(present));
+    uint8_t *hcode = (uint8_t *)(st->h_scalars + 16);          // 256 pinned bytes
+    uint32_t sigma = 0;
+    for (int c = 0; c < 256; c++) {
+        const bool p = (present[c >> 5] >> (c & 31)) & 1u;
+        hcode[c] = p ? (uint8_t)(++sigma) : 0;
+    }
+    const int bps = bits_for(sigma);                           // codes 0..sigma
+    const int h0 = 63 / bps;
+    uint8_t *dcode = slot<uint8_t>(st, S_TMP1, 256);
+    check_cuda(cudaMemcpyAsync(dcode, hcode, 256, cudaMemcpyHostToDevice, st->stream));
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, N);
-    k_dict_keys<<<grid_for(N, 256), 256, 0, st->stream>>>(ph.dict, N, rem, small, keys);
+    k_dict_keys<<<grid_for(N, 256), 256, 0, st->stream>>>(ph.dict, N, rem, dcode, bps, h0, keys);
     after_launch(st);
     dord.isa = slot<uint32_t>(st, S_ISA, N);
     dord.sa = slot<uint32_t>(st, S_SA, N);
-    dord.rounds = prefix_doubling(st, N, small ? 61 : 57, small ? DICT_H0_SMALL : DICT_H0, rem, dord.isa, dord.sa);
+    dord.rounds = prefix_doubling(st, N, h0 * bps + 1, (uint32_t)h0, rem, dord.isa, dord.sa);
     dord.lexrank = slot<uint32_t>(st, S_LEXRANK, ph.d);
     device_scan<uint32_t, OpAdd>(st, N, LoadIsStart{dord.sa, ph.dphr, ph.doff},
                                  StoreLexRank{dord.sa, ph.dphr, dord.lexrank}, false, (uint32_t *)nullptr);
