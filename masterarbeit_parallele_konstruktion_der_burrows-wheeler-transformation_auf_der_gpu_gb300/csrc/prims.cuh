@@ -189,13 +189,14 @@ __device__ __forceinline__ uint32_t rs_digit(K k, int shift, uint32_t mask)
     return (uint32_t)(k >> shift) & mask;
 }
 
-template <typename K>
+template <typename K, int BITS>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__ keys, uint32_t n, int shift,
                                                            uint32_t mask, uint32_t *__restrict__ tile_hist,
                                                            uint32_t num_tiles)
 {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    constexpr int D = 1 << BITS;
+    __shared__ uint32_t h[D];
+    for (int d = threadIdx.x; d < D; d += RS_THREADS) h[d] = 0;
     __syncthreads();
     size_t base = (size_t)blockIdx.x * RS_TILE;
 #pragma unroll 4
@@ -207,33 +208,35 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__
         if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    tile_hist[(size_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
+    for (int d = threadIdx.x; d < D; d += RS_THREADS) tile_hist[(size_t)d * num_tiles + blockIdx.x] = h[d];
 }
 
-template <typename K, bool HAS_VAL>
+template <typename K, bool HAS_VAL, int BITS>
 constexpr size_t rs_smem_bytes()
 {
-    return (size_t)RS_TILE * sizeof(K) + (HAS_VAL ? (size_t)RS_TILE * 4 : 0) + (size_t)RS_WARPS * 256 * 4 +
-           256 * 4 * 2 + 32 * 4;
+    return (size_t)RS_TILE * sizeof(K) + (HAS_VAL ? (size_t)RS_TILE * 4 : 0) + (size_t)RS_WARPS * (1 << BITS) * 4 +
+           (size_t)(1 << BITS) * 4 * 2 + 32 * 4;
 }
 
-template <typename K, bool HAS_VAL>
+template <typename K, bool HAS_VAL, int BITS>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict__ kin, K *__restrict__ kout,
                                                              const uint32_t *__restrict__ vin,
                                                              uint32_t *__restrict__ vout, uint32_t n, int shift,
                                                              uint32_t mask, const uint32_t *__restrict__ tile_off,
                                                              uint32_t num_tiles)
 {
+    constexpr int D = 1 << BITS;
+    constexpr int DPT = D / RS_THREADS;       // digits per thread in the per-digit phase
     extern __shared__ __align__(16) unsigned char rs_smem[];
     K *s_k = (K *)rs_smem;
     uint32_t *s_v = (uint32_t *)(s_k + RS_TILE);
     uint32_t *s_wh = HAS_VAL ? s_v + RS_TILE : s_v;
-    uint32_t *s_dstart = s_wh + RS_WARPS * 256;
-    uint32_t *s_goff = s_dstart + 256;
-    uint32_t *s_scan = s_goff + 256;
+    uint32_t *s_dstart = s_wh + RS_WARPS * D;
+    uint32_t *s_goff = s_dstart + D;
+    uint32_t *s_scan = s_goff + D;
 
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) s_wh[i] = 0;
+    for (int i = threadIdx.x; i < RS_WARPS * D; i += RS_THREADS) s_wh[i] = 0;
     __syncthreads();
 
     const size_t tile_base = (size_t)blockIdx.x * RS_TILE;
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
         if (HAS_VAL) v[i] = valid ? vin[idx] : 0u;
         dg[i] = valid ? rs_digit(k[i], shift, mask) : 0xFFFFFFFFu;
     }
-    uint32_t *wh = s_wh + warp * 256;
+    uint32_t *wh = s_wh + warp * D;
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; i++) {
         uint32_t d = dg[i];
@@ -267,24 +270,37 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
     }
     __syncthreads();
     {
-        const uint32_t d = threadIdx.x;
-        uint32_t run = 0;
+        // thread t owns digits [t*DPT, t*DPT + DPT)
+        uint32_t cnt[DPT];
+        uint32_t sum = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; w++) {
-            uint32_t c = s_wh[w * 256 + d];
-            s_wh[w * 256 + d] = run;
-            run += c;
+        for (int e = 0; e < DPT; e++) {
+            const uint32_t d = threadIdx.x * DPT + e;
+            uint32_t run = 0;
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; w++) {
+                uint32_t c = s_wh[w * D + d];
+                s_wh[w * D + d] = run;
+                run += c;
+            }
+            cnt[e] = run;
+            sum += run;
         }
         uint32_t total;
-        uint32_t ex = block_excl_scan<uint32_t, OpAdd>(run, total, OpAdd(), s_scan);
-        s_dstart[d] = ex;
-        s_goff[d] = tile_off[(size_t)d * num_tiles + blockIdx.x];
+        uint32_t ex = block_excl_scan<uint32_t, OpAdd>(sum, total, OpAdd(), s_scan);
+#pragma unroll
+        for (int e = 0; e < DPT; e++) {
+            const uint32_t d = threadIdx.x * DPT + e;
+            s_dstart[d] = ex;
+            ex += cnt[e];
+            s_goff[d] = tile_off[(size_t)d * num_tiles + blockIdx.x];
+        }
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; i++) {
         if (dg[i] != 0xFFFFFFFFu) {
-            uint32_t lp = s_dstart[dg[i]] + s_wh[warp * 256 + dg[i]] + rk[i];
+            uint32_t lp = s_dstart[dg[i]] + s_wh[warp * D + dg[i]] + rk[i];
             s_k[lp] = k[i];
             if (HAS_VAL) s_v[lp] = v[i];
         }
@@ -300,31 +316,35 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
     }
 }
 
-// Sorts (keys, vals) stably by bits [begin_bit, end_bit).  On return `keys`
-// and `vals` point at the sorted data (the *_alt buffers hold garbage).
-template <typename K, bool HAS_VAL>
+// Sorts (keys, vals) stably by bits [begin_bit, end_bit) with BITS-bit digits
+// (8: 256 buckets; 10: 1024 buckets, fewer passes for 17..20-bit keys).  On
+// return `keys` and `vals` point at the sorted data (the *_alt buffers hold
+// garbage).
+template <typename K, bool HAS_VAL, int BITS = 8>
 void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *&vals_alt, uint32_t n,
                 int begin_bit, int end_bit)
 {
+    static_assert((1 << BITS) % RS_THREADS == 0, "digit count must be a multiple of the CTA size");
     if (n <= 1 || end_bit <= begin_bit) return;
     static bool attr_set = false;
-    constexpr size_t smem = rs_smem_bytes<K, HAS_VAL>();
+    constexpr size_t smem = rs_smem_bytes<K, HAS_VAL, BITS>();
     if (!attr_set) {
-        check_cuda(cudaFuncSetAttribute(k_rs_downsweep<K, HAS_VAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+        check_cuda(cudaFuncSetAttribute(k_rs_downsweep<K, HAS_VAL, BITS>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    uint32_t num_tiles = (uint32_t)((n + RS_TILE - 1) / RS_TILE);
-    uint32_t *hist = slot<uint32_t>(st, S_RSHIST, (size_t)256 * num_tiles);
-    for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        int bits = end_bit - shift < 8 ? end_bit - shift : 8;
+    const uint32_t num_tiles = (uint32_t)((n + RS_TILE - 1) / RS_TILE);
+    const size_t D = (size_t)1 << BITS;
+    uint32_t *hist = slot<uint32_t>(st, S_RSHIST, D * num_tiles);
+    for (int shift = begin_bit; shift < end_bit; shift += BITS) {
+        int bits = end_bit - shift < BITS ? end_bit - shift : BITS;
         uint32_t mask = (1u << bits) - 1u;
-        k_rs_upsweep<K><<<num_tiles, RS_THREADS, 0, st->stream>>>(keys, n, shift, mask, hist, num_tiles);
+        k_rs_upsweep<K, BITS><<<num_tiles, RS_THREADS, 0, st->stream>>>(keys, n, shift, mask, hist, num_tiles);
         after_launch(st);
-        scan_array_excl<uint32_t, OpAdd>(st, hist, (size_t)256 * num_tiles, 0);
+        scan_array_excl<uint32_t, OpAdd>(st, hist, D * num_tiles, 0);
         probe_begin(st, GBWT_PROBE_RADIX_SCATTER);
-        k_rs_downsweep<K, HAS_VAL><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt, n,
-                                                                                shift, mask, hist, num_tiles);
+        k_rs_downsweep<K, HAS_VAL, BITS><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt,
+                                                                                      n, shift, mask, hist, num_tiles);
         probe_end(st, GBWT_PROBE_RADIX_SCATTER, (uint64_t)n * 2 * (sizeof(K) + (HAS_VAL ? 4 : 0)));
         after_launch(st);
         K *t = keys; keys = keys_alt; keys_alt = t;
