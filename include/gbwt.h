@@ -145,6 +145,18 @@ int64_t gbwt_pfp_parse(void *storage, const uint8_t *T, int64_t n, int32_t W, in
 int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, int32_t P, uint32_t flags,
                                       uint32_t *D, int64_t capacity, void *stream);
 
+/*
+ * libcubwt-compatible BWT (libcubwt.cuh:60-69, libcubwt.cu:2414-2431):
+ * L[0] = T[n-1], then the BWT of T$ without its '$' entry; returns the
+ * primary index (the row where '$' stood, >= 1).  T and L are host buffers.
+ * Any byte values are accepted: a text with at most 253 distinct values is
+ * mapped monotonically into [2,254] (which leaves its BWT unchanged), run
+ * through the PFP pipeline with W=5, P=16, and mapped back; a text using all
+ * 254-256 values gives GBWT_UNSUPPORTED_INPUT.  No counterpart in the
+ * reference's PFP programs; it serves callers of the vendored libcubwt.
+ */
+int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n);
+
 /* Copies the counts of the last call into *out. */
 int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
 

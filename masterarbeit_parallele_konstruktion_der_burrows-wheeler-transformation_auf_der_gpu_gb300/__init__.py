@@ -84,6 +84,7 @@ EXPORTS = (
     "gbwt_allocate_device_storage", "gbwt_free_device_storage", "gbwt_set_stream", "gbwt_pfp_bwt",
     "gbwt_pfp_trigger_scan", "gbwt_pfp_parse", "gbwt_get_stats", "gbwt_read_input_txt",
     "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
+    "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc",
 )
 
 PROBE_NONE = -1
@@ -128,6 +129,8 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_error_string.restype = ctypes.c_char_p
     L.gbwt_set_kernel_probe.argtypes = [vp, i32]
     L.gbwt_set_kernel_probe.restype = i64
+    L.gbwt_libcubwt_bwt.argtypes = [vp, u8p, u8p, i64]
+    L.gbwt_libcubwt_bwt.restype = i64
     _LIB = L
     return L
 
@@ -203,6 +206,15 @@ class Storage:
         flags = FLAG_SMALL_ALPHABET if small_alphabet else 0
         return _check(_lib().gbwt_pfp_bwt(self.handle, text.ctypes.data, out.ctypes.data, len(text), W, P, flags),
                       "gbwt_pfp_bwt")
+
+    def libcubwt_bwt(self, text) -> tuple[np.ndarray, int]:
+        """libcubwt_bwt semantics (any byte values, <= 253 distinct): returns
+        (L, primary index) with L[0] = T[n-1] and the '$' entry removed."""
+        t = _host_u8(text)
+        out = np.empty(max(len(t), 1), dtype=np.uint8)
+        idx = _check(_lib().gbwt_libcubwt_bwt(self.handle, t.ctypes.data, out.ctypes.data, len(t)),
+                     "gbwt_libcubwt_bwt")
+        return out[:len(t)], idx
 
     def set_kernel_probe(self, kernel: int) -> None:
         """Time every launch of one kernel family (PROBE_*) from now on."""

@@ -190,7 +190,7 @@ extern "C" int64_t gbwt_allocate_device_storage(void **storage, int64_t max_leng
         st->stream = st->own_stream;
         check_cuda(cudaMalloc(&st->d_flags, 64 * sizeof(uint32_t)));
         check_cuda(cudaMalloc(&st->d_scalars, 64 * sizeof(uint64_t)));
-        check_cuda(cudaHostAlloc(&st->h_scalars, 64 * sizeof(uint64_t), cudaHostAllocDefault));
+        check_cuda(cudaHostAlloc(&st->h_scalars, 256 * sizeof(uint64_t), cudaHostAllocDefault));
         for (int i = 0; i < 10; i++) check_cuda(cudaEventCreate(&st->ev[i]));
         st->max_length = max_length;
         if (max_length > 0) {
@@ -291,6 +291,109 @@ extern "C" int64_t gbwt_set_kernel_probe(void *storage, int32_t kernel)
         st->probe_ms = 0.0;
         return GBWT_NO_ERROR;
     });
+}
+
+// ---- libcubwt-compatible entry point ----------------------------------
+namespace gbwt {
+
+__global__ void k_byte_presence(const uint8_t *T, uint32_t n, uint32_t *bits)
+{
+    uint32_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = T[i];
+#pragma unroll
+        for (int w = 0; w < 8; w++) m[w] |= ((c >> 5) == (uint32_t)w) ? (1u << (c & 31u)) : 0u;
+    }
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+        const uint32_t v = __reduce_or_sync(0xFFFFFFFFu, m[w]);
+        if ((threadIdx.x & 31u) == 0 && v) atomicOr(bits + w, v);
+    }
+}
+
+// buf[i] = map[buf[i]]
+__global__ void k_byte_map(uint8_t *buf, uint32_t n, const uint8_t *map)
+{
+    __shared__ uint8_t s_map[256];
+    s_map[threadIdx.x] = map[threadIdx.x];      // blockDim == 256
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) buf[i] = s_map[buf[i]];
+}
+
+// libcubwt layout: L[0] = last, L[i] = O[i-1] for 1 <= i <= pidx, L[i] = O[i]
+// after it (the reference convention's row pidx is libcubwt's '$' row).
+__global__ void k_libcubwt_layout(const uint8_t *O, uint8_t *L, uint32_t n, uint32_t pidx, const uint8_t *unmap,
+                                  uint8_t last)
+{
+    __shared__ uint8_t s_un[256];
+    s_un[threadIdx.x] = unmap[threadIdx.x];      // blockDim == 256
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (i == 0) L[0] = last;
+        else L[i] = s_un[i <= pidx ? O[i - 1] : O[i]];
+    }
+}
+
+static int64_t libcubwt_bwt(Storage *st, const uint8_t *T, uint8_t *L, int64_t n)
+{
+    const uint32_t un = (uint32_t)n;
+    uint8_t *dT = slot<uint8_t>(st, S_TEXT, (size_t)n + 16);
+    check_cuda(cudaMemcpyAsync(dT, T, (size_t)n, cudaMemcpyHostToDevice, st->stream));
+    check_cuda(cudaMemsetAsync(st->d_flags + 8, 0, 8 * sizeof(uint32_t), st->stream));
+    unsigned grid = grid_for(un, 256);
+    if (grid > (unsigned)st->num_sms * 8) grid = (unsigned)st->num_sms * 8;
+    k_byte_presence<<<grid, 256, 0, st->stream>>>(dT, un, st->d_flags + 8);
+    after_launch(st);
+    uint32_t present[8];
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 4, st->d_flags + 8, sizeof(present), cudaMemcpyDeviceToHost,
+                               st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    memcpy(present, st->h_scalars + 4, sizeof(present));
+    uint8_t *hmap = (uint8_t *)(st->h_scalars + 16);           // 256 pinned bytes each
+    uint8_t *hunmap = (uint8_t *)(st->h_scalars + 48);
+    uint32_t sigma = 0;
+    bool identity = true;
+    for (int c = 0; c < 256; c++) {
+        hmap[c] = 0;
+        hunmap[c] = (uint8_t)c;
+    }
+    for (int c = 0; c < 256; c++) {
+        if ((present[c >> 5] >> (c & 31)) & 1u) {
+            const uint32_t code = 2 + sigma++;
+            if (code > 254) return GBWT_UNSUPPORTED_INPUT;      // 254..256 distinct values
+            hmap[c] = (uint8_t)code;
+            hunmap[code] = (uint8_t)c;
+            if (c < 2 || c > 254) identity = false;
+        }
+    }
+    uint8_t *dmaps = slot<uint8_t>(st, S_LCBMAP, 512);     // not touched by the pipeline
+    if (!identity) {
+        check_cuda(cudaMemcpyAsync(dmaps, hmap, 256, cudaMemcpyHostToDevice, st->stream));
+        k_byte_map<<<grid, 256, 0, st->stream>>>(dT, un, dmaps);
+        after_launch(st);
+    } else {
+        for (int c = 0; c < 256; c++) hunmap[c] = (uint8_t)c;
+    }
+    check_cuda(cudaMemcpyAsync(dmaps + 256, hunmap, 256, cudaMemcpyHostToDevice, st->stream));
+    uint8_t *dO = slot<uint8_t>(st, S_OUT, (size_t)n + 16);
+    int64_t rc = pipeline(st, dT, dO, n, 5, 16, GBWT_FLAG_DEVICE_POINTERS, UPTO_BWT, nullptr);
+    if (rc < 0) return rc;
+    const uint32_t pidx = (uint32_t)st->stats.primary_index;
+    uint8_t *dL = slot<uint8_t>(st, S_LCB, (size_t)n + 16);
+    k_libcubwt_layout<<<grid, 256, 0, st->stream>>>(dO, dL, un, pidx, dmaps + 256, T[n - 1]);
+    after_launch(st);
+    check_cuda(cudaMemcpyAsync(L, dL, (size_t)n, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    return (int64_t)pidx + 1;
+}
+
+}  // namespace gbwt
+
+extern "C" int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n)
+{
+    Storage *st = (Storage *)storage;
+    if (!st || !T || !L || n < 1 || n > MAX_N) return GBWT_BAD_PARAMETER;
+    return guarded([&]() { return libcubwt_bwt(st, T, L, n); });
 }
 
 extern "C" int64_t gbwt_get_stats(void *storage, gbwt_stats *out)

@@ -29,6 +29,7 @@ int main(int argc, char **argv)
     int W = 5, P = 16;
     bool small = false;
     std::string in = "input.txt", out = "out.txt";
+    std::string bin_in, bin_out;          // raw-byte fast path instead of decimal text
     std::string self = argv[0];
     size_t slash = self.find_last_of('/');
     if (slash != std::string::npos) self = self.substr(slash + 1);
@@ -40,17 +41,35 @@ int main(int argc, char **argv)
         else if (a == "--small") small = true;
         else if (a == "--in" && i + 1 < argc) in = argv[++i];
         else if (a == "--out" && i + 1 < argc) out = argv[++i];
+        else if (a == "--binary-in" && i + 1 < argc) bin_in = argv[++i];
+        else if (a == "--binary-out" && i + 1 < argc) bin_out = argv[++i];
         else if (a == "--variant" && i + 1 < argc) {
             if (!parse_variant(argv[++i], W, P, small)) { fprintf(stderr, "bad variant name\n"); return 2; }
         } else {
-            fprintf(stderr, "usage: %s [--W w --P p --small] [--variant NAME] [--in input.txt] [--out out.txt]\n",
+            fprintf(stderr, "usage: %s [--W w --P p --small] [--variant NAME] [--in input.txt] [--out out.txt]"
+                            " [--binary-in FILE] [--binary-out FILE]\n",
                     argv[0]);
             return 2;
         }
     }
     uint8_t *T = nullptr;
     int64_t n = 0;
-    int64_t rc = gbwt_read_input_txt(in.c_str(), &T, &n);
+    int64_t rc;
+    if (!bin_in.empty()) {
+        // raw bytes: no decimal parsing (the reference's fscanf loop dominates
+        // its wall time on large inputs, K:111-150)
+        FILE *f = fopen(bin_in.c_str(), "rb");
+        if (!f) { fprintf(stderr, "gbwt_pfp: cannot open %s\n", bin_in.c_str()); return 1; }
+        fseek(f, 0, SEEK_END);
+        long sz = ftell(f);
+        fseek(f, 0, SEEK_SET);
+        T = (uint8_t *)malloc(sz > 0 ? (size_t)sz : 1);
+        n = (int64_t)fread(T, 1, sz > 0 ? (size_t)sz : 0, f);
+        fclose(f);
+        rc = n;
+    } else {
+        rc = gbwt_read_input_txt(in.c_str(), &T, &n);
+    }
     if (rc < 0) { fprintf(stderr, "gbwt_pfp: cannot read %s: %s\n", in.c_str(), gbwt_error_string(rc)); return 1; }
     void *st = nullptr;
     rc = gbwt_allocate_device_storage(&st, n);
@@ -64,7 +83,13 @@ int main(int argc, char **argv)
         free(L);
         return 1;
     }
-    rc = gbwt_write_out_txt(out.c_str(), L, n);
+    if (!bin_out.empty()) {
+        FILE *f = fopen(bin_out.c_str(), "wb");
+        rc = (f && fwrite(L, 1, (size_t)n, f) == (size_t)n) ? n : -1;
+        if (f) fclose(f);
+    } else {
+        rc = gbwt_write_out_txt(out.c_str(), L, n);
+    }
     gbwt_free_device_storage(st);
     gbwt_free_host(T);
     free(L);

@@ -31,7 +31,7 @@ enum Slot : int {
     S_GCOUNT, S_GCHAR, S_GMIX, S_GOFF, S_GRP, S_MOFF, S_MB, S_MC, S_MIXIDX, S_DELTA,
     S_ELEM0, S_ELEM1,
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
-    S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2,
+    S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2, S_LCB, S_LCBMAP,
     S_NUM
 };
 
@@ -44,7 +44,7 @@ struct Storage {
     int64_t max_length = 0;
     Buf slots[S_NUM];
     uint32_t *d_flags = nullptr;        // [0] error bits, [1..] counters
-    uint64_t *h_scalars = nullptr;      // pinned host mirror (64 entries)
+    uint64_t *h_scalars = nullptr;      // pinned host mirror (256 entries; [16..80) byte tables)
     uint64_t *d_scalars = nullptr;      // device scalars (64 entries)
     gbwt_stats stats;
     int64_t launches = 0;

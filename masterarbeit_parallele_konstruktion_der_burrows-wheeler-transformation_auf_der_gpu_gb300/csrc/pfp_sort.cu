@@ -282,7 +282,8 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
                                                             const uint32_t *__restrict__ act_g,
                                                             const uint32_t *__restrict__ key2, uint32_t A, uint32_t h2,
                                                             Rem rem, uint32_t *isa, uint32_t *sa, uint32_t *out_x,
-                                                            uint32_t *out_g, uint32_t *counter, uint32_t *flags)
+                                                            uint32_t *out_g, uint32_t *counter, uint32_t *flags,
+                                                            bool collect_stats)
 {
     extern __shared__ __align__(16) unsigned char ss_smem[];
     uint64_t *s_key = (uint64_t *)ss_smem;           // (isa[x+h]+1) << 32 | local index
@@ -348,8 +349,26 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     __syncthreads();
 
     // Tier 3: groups larger than SS_WARPMAX are sorted by the whole CTA.
-    for (uint32_t sg = threadIdx.x; sg < nsegs; sg += SS_THREADS)
-        if (s_ss[sg + 1] - s_ss[sg] > SS_WARPMAX) s_big[atomicAdd(&s_misc[3], 1u)] = sg;
+    // flags[16..19] accumulate group statistics per tier (elements in groups
+    // <= SS_COUNTMAX, <= SS_WARPMAX, larger; number of groups).
+    uint32_t e1c = 0, e2c = 0, e3c = 0;
+    for (uint32_t sg = threadIdx.x; sg < nsegs; sg += SS_THREADS) {
+        const uint32_t s = s_ss[sg + 1] - s_ss[sg];
+        if (s > SS_WARPMAX) { s_big[atomicAdd(&s_misc[3], 1u)] = sg; e3c += s; }
+        else if (s > SS_COUNTMAX) e2c += s;
+        else e1c += s;
+    }
+    if (collect_stats) {
+        e1c = __reduce_add_sync(0xFFFFFFFFu, e1c);
+        e2c = __reduce_add_sync(0xFFFFFFFFu, e2c);
+        e3c = __reduce_add_sync(0xFFFFFFFFu, e3c);
+        if ((threadIdx.x & 31u) == 0) {
+            if (e1c) atomicAdd(flags + 16, e1c);
+            if (e2c) atomicAdd(flags + 17, e2c);
+            if (e3c) atomicAdd(flags + 18, e3c);
+        }
+        if (threadIdx.x == 0) atomicAdd(flags + 19, nsegs);
+    }
     __syncthreads();
     const uint32_t nbig = s_misc[3];
     for (uint32_t b = 0; b < nbig; b++) {
@@ -396,6 +415,56 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         const uint32_t ss = s_ss[sg], se = s_ss[sg + 1], s = se - ss;
         const uint32_t g = s_sg[sg];
         uint64_t *key = s_key + ss;
+        // Fast paths for groups whose isa[x+h] takes one or two values (most
+        // groups of a repetitive text in early rounds): a stable partition
+        // in input order replaces the sort.
+        uint32_t mn = 0xFFFFFFFFu, mx = 0;
+        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+            const uint32_t i = c0 + lane;
+            if (i < s) {
+                const uint32_t k2 = (uint32_t)(key[i] >> 32);
+                mn = min(mn, k2);
+                mx = max(mx, k2);
+            }
+        }
+        mn = __reduce_min_sync(0xFFFFFFFFu, mn);
+        mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+        bool two = mn != mx;
+        uint32_t cmn = 0;                    // members with the smaller value
+        if (two) {
+            bool other = false;
+            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+                const uint32_t i = c0 + lane;
+                const uint32_t k2 = i < s ? (uint32_t)(key[i] >> 32) : mn;
+                other |= (k2 != mn && k2 != mx);
+                cmn += __popc(__ballot_sync(0xFFFFFFFFu, i < s && k2 == mn));
+            }
+            two = !__any_sync(0xFFFFFFFFu, other);
+        }
+        if (mn == mx || two) {
+            uint32_t rmn = 0, rmx = 0;       // running ranks among equal members
+            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+                const uint32_t i = c0 + lane;
+                const bool in = i < s;
+                const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : 0u;
+                const bool lo = in && k2 == mn;
+                const unsigned blo = __ballot_sync(0xFFFFFFFFu, lo), bhi = __ballot_sync(0xFFFFFFFFu, in && !lo);
+                const unsigned lt = (1u << lane) - 1u;
+                if (in) {
+                    const uint32_t li = (uint32_t)key[i] & 0xFFFFu;
+                    uint32_t pos, nh;
+                    bool single;
+                    if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = (mn == mx ? s : cmn) == 1; }
+                    else { pos = cmn + rmx + __popc(bhi & lt); nh = g + cmn; single = s - cmn == 1; }
+                    const bool done = single || rem(s_x[li]) <= h2;
+                    s_nh[ss + pos] = nh | (done ? 0x80000000u : 0u);
+                    s_perm[ss + pos] = (uint16_t)li;
+                }
+                rmn += __popc(blo);
+                rmx += __popc(bhi);
+            }
+            continue;
+        }
         if (s <= 32) warp_sort_regs<1>(key, s, lane);
         else if (s <= 64) warp_sort_regs<2>(key, s, lane);
         else if (s <= 128) warp_sort_regs<4>(key, s, lane);
@@ -509,10 +578,17 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         if (!big) {
             uint32_t *counter = (uint32_t *)st->d_scalars;
             check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+            if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 4 * sizeof(uint32_t), st->stream));
             k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
-                act_x, act_g, key2, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags);
+                act_x, act_g, key2, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags, debug);
             after_launch(st);
             fetch_scalars(st, 1);
+            if (debug) {
+                uint32_t tiers[4];
+                check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
+                fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
+                        SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
+            }
             A = (uint32_t)st->h_scalars[0];
             uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
             uint32_t *t2 = act_g; act_g = act_g2; act_g2 = t2;
