@@ -108,6 +108,19 @@ int64_t gbwt_pfp_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n,
                      int32_t W, int32_t P, uint32_t flags);
 
 /*
+ * PFP BWT of k independent texts in one pipeline run.  Text t is
+ * T_concat[offsets[t] .. offsets[t+1]) (offsets[0] = 0, non-decreasing,
+ * HOST array of k+1 entries); its BWT, exactly what gbwt_pfp_bwt returns for
+ * it alone, is written to L_concat at the same offsets.  Empty texts are
+ * allowed and produce nothing.  No counterpart in the reference, which
+ * builds one BWT per process run (main(), K:4793-4815); a caller of the
+ * reference runs the program once per text.  With GBWT_FLAG_DEVICE_POINTERS
+ * T_concat and L_concat are device pointers.  Returns offsets[k].
+ */
+int64_t gbwt_pfp_bwt_batch(void *storage, const uint8_t *T_concat, const int64_t *offsets, int32_t k,
+                           uint8_t *L_concat, int32_t W, int32_t P, uint32_t flags);
+
+/*
  * Trigger scan only: writes the phrase end positions D[0..z) (the last is
  * n+W-1) and returns z.  Replaces Compute_D1/D2/D3 (K:443-576, driver
  * K:2415-2455).  Returns GBWT_BAD_PARAMETER when capacity < z.

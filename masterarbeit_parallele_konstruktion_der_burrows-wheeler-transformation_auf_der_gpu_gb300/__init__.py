@@ -84,7 +84,7 @@ EXPORTS = (
     "gbwt_allocate_device_storage", "gbwt_free_device_storage", "gbwt_set_stream", "gbwt_pfp_bwt",
     "gbwt_pfp_trigger_scan", "gbwt_pfp_parse", "gbwt_get_stats", "gbwt_read_input_txt",
     "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
-    "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc",
+    "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch",
 )
 
 PROBE_NONE = -1
@@ -131,6 +131,8 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_set_kernel_probe.restype = i64
     L.gbwt_libcubwt_bwt.argtypes = [vp, u8p, u8p, i64]
     L.gbwt_libcubwt_bwt.restype = i64
+    L.gbwt_pfp_bwt_batch.argtypes = [vp, u8p, ctypes.c_void_p, i32, u8p, i32, i32, u32]
+    L.gbwt_pfp_bwt_batch.restype = i64
     _LIB = L
     return L
 
@@ -206,6 +208,40 @@ class Storage:
         flags = FLAG_SMALL_ALPHABET if small_alphabet else 0
         return _check(_lib().gbwt_pfp_bwt(self.handle, text.ctypes.data, out.ctypes.data, len(text), W, P, flags),
                       "gbwt_pfp_bwt")
+
+    def pfp_bwt_batch(self, texts, W: int = 5, P: int = 16, small_alphabet: bool = False,
+                      stage_times: bool = False) -> list[np.ndarray]:
+        """BWTs of many texts in one pipeline run; each equals pfp_bwt(text)."""
+        parts = [_host_u8(t) for t in texts]
+        offsets = np.zeros(len(parts) + 1, dtype=np.int64)
+        np.cumsum([len(t) for t in parts], out=offsets[1:])
+        concat = np.concatenate(parts) if parts else np.zeros(0, dtype=np.uint8)
+        out = np.empty(max(len(concat), 1), dtype=np.uint8)
+        self.pfp_bwt_batch_into(concat, offsets, out, W, P, small_alphabet, stage_times)
+        return [out[offsets[i]:offsets[i + 1]] for i in range(len(parts))]
+
+    def pfp_bwt_batch_into(self, concat: np.ndarray, offsets: np.ndarray, out: np.ndarray, W: int = 5,
+                           P: int = 16, small_alphabet: bool = False, stage_times: bool = False) -> int:
+        """Concatenated texts with int64 offsets[k+1] (host arrays) -> out at the same offsets."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        if concat.dtype != np.uint8 or out.dtype != np.uint8 or not concat.flags.c_contiguous \
+                or not out.flags.c_contiguous or len(offsets) < 1 or len(out) < offsets[-1] \
+                or len(concat) < offsets[-1]:
+            raise ValueError("concat/out must be contiguous uint8 arrays covering offsets[-1] bytes")
+        flags = (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (FLAG_STAGE_TIMES if stage_times else 0)
+        return _check(_lib().gbwt_pfp_bwt_batch(self.handle, concat.ctypes.data, offsets.ctypes.data,
+                                                len(offsets) - 1, out.ctypes.data, W, P, flags),
+                      "gbwt_pfp_bwt_batch")
+
+    def pfp_bwt_batch_device(self, text_ptr: int, offsets: np.ndarray, out_ptr: int, W: int = 5, P: int = 16,
+                             small_alphabet: bool = False, stage_times: bool = False) -> int:
+        """Device-pointer batch: text_ptr/out_ptr are CUDA addresses, offsets a host int64 array."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        flags = FLAG_DEVICE_POINTERS | (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (
+            FLAG_STAGE_TIMES if stage_times else 0)
+        return _check(_lib().gbwt_pfp_bwt_batch(self.handle, ctypes.c_void_p(text_ptr), offsets.ctypes.data,
+                                                len(offsets) - 1, ctypes.c_void_p(out_ptr), W, P, flags),
+                      "gbwt_pfp_bwt_batch")
 
     def libcubwt_bwt(self, text) -> tuple[np.ndarray, int]:
         """libcubwt_bwt semantics (any byte values, <= 253 distinct): returns

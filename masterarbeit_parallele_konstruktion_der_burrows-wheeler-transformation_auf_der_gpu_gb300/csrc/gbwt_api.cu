@@ -221,6 +221,7 @@ extern "C" int64_t gbwt_free_device_storage(void *storage)
     if (st->d_flags) cudaFree(st->d_flags);
     if (st->d_scalars) cudaFree(st->d_scalars);
     if (st->h_scalars) cudaFreeHost(st->h_scalars);
+    if (st->h_meta) cudaFreeHost(st->h_meta);
     for (int i = 0; i < 10; i++)
         if (st->ev[i]) cudaEventDestroy(st->ev[i]);
     for (int i = 0; i < 2 * st->probe_cap; i++) cudaEventDestroy(st->probe_ev[i]);
@@ -244,6 +245,14 @@ extern "C" int64_t gbwt_pfp_bwt(void *storage, const uint8_t *T, uint8_t *L, int
     Storage *st = (Storage *)storage;
     if (!st) return GBWT_BAD_PARAMETER;
     return guarded([&]() { return pipeline(st, T, L, n, W, P, flags, UPTO_BWT, nullptr); });
+}
+
+extern "C" int64_t gbwt_pfp_bwt_batch(void *storage, const uint8_t *T_concat, const int64_t *offsets, int32_t k,
+                                      uint8_t *L_concat, int32_t W, int32_t P, uint32_t flags)
+{
+    Storage *st = (Storage *)storage;
+    if (!st) return GBWT_BAD_PARAMETER;
+    return guarded([&]() { return run_batch(st, T_concat, offsets, k, L_concat, W, P, flags, MAX_N); });
 }
 
 extern "C" int64_t gbwt_pfp_trigger_scan(void *storage, const uint8_t *T, int64_t n, int32_t W, int32_t P,

@@ -32,6 +32,7 @@ enum Slot : int {
     S_ELEM0, S_ELEM1,
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
     S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2, S_LCB, S_LCBMAP,
+    S_BX, S_BMETA, S_BTID, S_BZEND, S_BLAST,
     S_NUM
 };
 
@@ -46,6 +47,8 @@ struct Storage {
     uint32_t *d_flags = nullptr;        // [0] error bits, [1..] counters
     uint64_t *h_scalars = nullptr;      // pinned host mirror (256 entries; [16..80) byte tables)
     uint64_t *d_scalars = nullptr;      // device scalars (64 entries)
+    uint32_t *h_meta = nullptr;         // pinned batch layout (grows on demand)
+    size_t h_meta_cap = 0;
     gbwt_stats stats;
     int64_t launches = 0;
     bool stage_times = false;
@@ -179,7 +182,17 @@ struct Phrases {
     uint8_t *dict = nullptr;           // [dict_bytes] concatenated phrases
     uint32_t *dphr = nullptr;          // [dict_bytes] phrase id per position
 };
-void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph);
+// A batch of texts laid out in one padded buffer X: text t at xstart[t],
+// followed by W sentinel bytes (value 1) that no text byte can take.  A
+// phrase whose predecessor ends on a sentinel starts the next text.
+struct BatchText {
+    uint32_t k = 0;                    // texts (all non-empty)
+    const uint32_t *xstart = nullptr;  // [k+1] text starts in X (xstart[k] = N)
+    const uint32_t *ptid = nullptr;    // [z] text of each phrase
+    const uint32_t *zend = nullptr;    // [k] one past the last phrase of each text
+    const uint8_t *lastb = nullptr;    // [k] last byte of each text
+};
+void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, const BatchText *bt = nullptr);
 
 struct DictOrder {
     uint32_t *isa = nullptr;     // [dict_bytes] final group head per position
@@ -195,10 +208,17 @@ struct ParseOrder {
     int rounds = 0;
 };
 void run_parse_sa(Storage *st, Phrases &ph, DictOrder &dord, ParseOrder &pord);
+void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchText &bt, ParseOrder &pord);
+// Group index of every dictionary position that starts a suffix longer than
+// W (equal suffixes share one group; groups numbered in dictionary order).
+uint32_t run_group_index(Storage *st, Phrases &ph, DictOrder &dord, int W, uint32_t *&grp_of);
 
 void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph,
                   DictOrder &dord, ParseOrder &pord, uint8_t *dOut);
 
 void stage_mark(Storage *st, int idx);
+
+int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t k, uint8_t *L, int W, int P,
+                  uint32_t flags, int64_t max_n);
 
 }  // namespace gbwt

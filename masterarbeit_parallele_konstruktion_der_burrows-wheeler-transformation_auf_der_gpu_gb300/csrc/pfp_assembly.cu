@@ -74,6 +74,20 @@ struct StoreSGroup {
     }
 };
 
+// Group index only (the batched assembly counts per text, not per group).
+struct StoreGroupOnly {
+    const uint32_t *sa;
+    PosInfo pi;
+    uint32_t W;
+    uint32_t *grp_of;
+    __device__ __forceinline__ void operator()(size_t t, uint32_t inc, uint32_t) const
+    {
+        uint32_t x = sa[t], q, off, rem;
+        pi.get(x, q, off, rem);
+        if (rem > W) grp_of[x] = inc - 1u;
+    }
+};
+
 // Pass 2 over dictionary positions: mark groups with differing bytes.
 __global__ void k_mark_mixed(uint32_t N, PosInfo pi, uint32_t W, const uint8_t *dict, const uint32_t *pcmin,
                              const uint32_t *pcmax, const uint32_t *grp_of, const uint16_t *gchar, uint8_t *gmix)
@@ -359,6 +373,18 @@ static void mixed_blocks(Storage *st, const uint8_t *dT, uint32_t n, int W, Phra
     k_mixed_scatter<E><<<grid_for((M + 3) / 4, 256), 256, 0, st->stream>>>(elem, M, delta, B, dOut, n, st->d_flags);
     probe_end(st, GBWT_PROBE_MIXED_SCATTER, (uint64_t)M * (sizeof(E) + 1));
     after_launch(st);
+}
+
+uint32_t run_group_index(Storage *st, Phrases &ph, DictOrder &dord, int W, uint32_t *&grp_of)
+{
+    const uint32_t N = (uint32_t)ph.dict_bytes;
+    PosInfo pi{ph.dphr, ph.doff, ph.dlen};
+    grp_of = slot<uint32_t>(st, S_GRP, N);
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, N, LoadSHead{dord.sa, dord.isa, pi, (uint32_t)W},
+                                 StoreGroupOnly{dord.sa, pi, (uint32_t)W, grp_of}, true, (uint32_t *)st->d_scalars);
+    fetch_scalars(st, 1);
+    return (uint32_t)st->h_scalars[0];
 }
 
 void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, DictOrder &dord,

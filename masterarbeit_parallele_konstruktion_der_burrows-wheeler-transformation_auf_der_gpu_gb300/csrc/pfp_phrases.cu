@@ -22,10 +22,17 @@ constexpr int PH_THREADS = 256;
 constexpr int PH_SPAN = 24576;
 constexpr uint64_t M61 = (1ull << 61) - 1ull;
 
-__device__ __forceinline__ void phrase_span(const uint32_t *D, uint32_t k, int W, uint32_t &start, uint32_t &end)
+// Phrase k spans [start, end]: end = D[k]; start = D[k-1]-W+1 (consecutive
+// phrases overlap by W, K:578-592).  In a batch of texts (xsep = the padded
+// buffer, see pfp_batch.cu) a phrase whose predecessor ended on a sentinel byte
+// is the first phrase of the next text and starts right after it.
+__device__ __forceinline__ void phrase_span(const uint32_t *D, uint32_t k, int W, const uint8_t *xsep,
+                                            uint32_t &start, uint32_t &end)
 {
     end = D[k];
-    start = k ? D[k - 1] - (uint32_t)W + 1u : 0u;
+    if (!k) { start = 0; return; }
+    const uint32_t p = D[k - 1];
+    start = (xsep && xsep[p] == 1) ? p + 1u : p - (uint32_t)W + 1u;
 }
 
 __device__ __forceinline__ uint64_t mulmod61(uint64_t a, uint64_t b)
@@ -50,6 +57,7 @@ struct HashArgs {
     uint32_t limit;         // distinct keys allowed before ERR_TABLE_FULL
     uint32_t *slot_of;
     uint32_t *flags;
+    const uint8_t *xsep;    // batch: padded text buffer, else null
 };
 
 __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
@@ -83,7 +91,7 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     const uint32_t k = k0 + threadIdx.x;
     if (k >= a.z) return;
     uint32_t start, end;
-    phrase_span(a.D, k, a.W, start, end);
+    phrase_span(a.D, k, a.W, a.xsep, start, end);
     const uint32_t len = end - start + 1u;
     // polynomial over little-endian 4-byte chunks (the last one zero-padded)
     uint64_t h = 0;
@@ -132,7 +140,8 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
 
 // Compares each occurrence with its representative; marks representatives.
 __global__ void k_phrase_verify(const uint8_t *T, uint32_t n, const uint32_t *D, uint32_t z, int W,
-                                const uint32_t *tvals, const uint32_t *slot_of, uint32_t *isrep, uint32_t *flags)
+                                const uint32_t *tvals, const uint32_t *slot_of, uint32_t *isrep, uint32_t *flags,
+                                const uint8_t *xsep)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= z) return;
@@ -141,8 +150,8 @@ __global__ void k_phrase_verify(const uint8_t *T, uint32_t n, const uint32_t *D,
     if (rep == k) return;
     if (rep >= z) { atomicOr(flags, ERR_COLLISION); return; }
     uint32_t s1, e1, s2, e2;
-    phrase_span(D, k, W, s1, e1);
-    phrase_span(D, rep, W, s2, e2);
+    phrase_span(D, k, W, xsep, s1, e1);
+    phrase_span(D, rep, W, xsep, s2, e2);
     if (e1 - s1 != e2 - s2) { atomicOr(flags, ERR_COLLISION); return; }
     const uint32_t len = e1 - s1 + 1u;
     for (uint32_t i = 0; i < len; i++) {
@@ -163,11 +172,12 @@ struct StoreDense {
     uint32_t *dlen;
     uint32_t *dstart;
     int W;
+    const uint8_t *xsep;
     __device__ __forceinline__ void operator()(size_t k, uint32_t pre, uint32_t v) const
     {
         if (!v) return;
         uint32_t s, e;
-        phrase_span(D, (uint32_t)k, W, s, e);
+        phrase_span(D, (uint32_t)k, W, xsep, s, e);
         tdense[slot_of[k]] = pre;
         dlen[pre] = e - s + 1u;
         dstart[pre] = s;
@@ -178,7 +188,8 @@ struct StoreDense {
 // every distinct phrase (warp-aggregated over equal ids).
 __global__ void k_phrase_finalize(const uint8_t *T, uint32_t n, const uint32_t *D, uint32_t z, int W,
                                   const uint32_t *slot_of, const uint32_t *tdense, uint32_t *pid, uint32_t *pidpc,
-                                  uint32_t *occ, uint32_t *pcmin, uint32_t *pcmax)
+                                  uint32_t *occ, uint32_t *pcmin, uint32_t *pcmax, const uint8_t *xsep,
+                                  const uint32_t *ptid, const uint8_t *lastb)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = k < z;
@@ -187,8 +198,10 @@ __global__ void k_phrase_finalize(const uint8_t *T, uint32_t n, const uint32_t *
         id = tdense[slot_of[k]];
         pid[k] = id;
         uint32_t s, e;
-        phrase_span(D, k, W, s, e);
-        c = preceding_byte(T, n, s);
+        phrase_span(D, k, W, xsep, s, e);
+        // the first phrase of a text is preceded by the text's last byte
+        if (xsep && (k == 0 || xsep[D[k - 1]] == 1)) c = lastb[ptid[k]];
+        else c = preceding_byte(T, n, s);
         if (pidpc) pidpc[k] = (id << 8) | c;     // only when ids fit 24 bits
     }
     const unsigned peers = __match_any_sync(0xFFFFFFFFu, id);
@@ -232,8 +245,9 @@ static uint32_t pow2_at_least(uint64_t v)
     return (uint32_t)c;
 }
 
-void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph)
+void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, const BatchText *bt)
 {
+    const uint8_t *xsep = bt ? dT : nullptr;
     const uint32_t z = ph.z;
     uint32_t *slot_of = slot<uint32_t>(st, S_SLOT, z);
     uint32_t *isrep = slot<uint32_t>(st, S_PID, z);     // reused for pid below
@@ -261,16 +275,16 @@ void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph)
         while ((1u << logc) < c) logc++;
         a.logc = logc;
         a.limit = (uint32_t)(((uint64_t)c * 3) / 4);
-        a.slot_of = slot_of; a.flags = st->d_flags;
+        a.slot_of = slot_of; a.flags = st->d_flags; a.xsep = xsep;
         probe_begin(st, GBWT_PROBE_PHRASE_HASH);
         k_phrase_hash<<<grid_for(z, PH_THREADS), PH_THREADS, 0, st->stream>>>(a);
         // text bytes of all phrases (n + (W-1)(z-1) overlap) + D read + slot write
         probe_end(st, GBWT_PROBE_PHRASE_HASH, (uint64_t)n + (uint64_t)(W - 1) * (z - 1) + 8ull * z);
         after_launch(st);
         k_phrase_verify<<<grid_for(z, 256), 256, 0, st->stream>>>(dT, n, ph.D, z, W, tvals, slot_of, isrep,
-                                                                  st->d_flags);
+                                                                  st->d_flags, xsep);
         after_launch(st);
-        device_scan<uint32_t, OpAdd>(st, z, LoadU32{isrep}, StoreDense{ph.D, slot_of, tdense, dlen, dstart, W},
+        device_scan<uint32_t, OpAdd>(st, z, LoadU32{isrep}, StoreDense{ph.D, slot_of, tdense, dlen, dstart, W, xsep},
                                      false, (uint32_t *)st->d_scalars);
         check_cuda(cudaMemcpyAsync(st->h_scalars + 1, st->d_flags, 4, cudaMemcpyDeviceToHost, st->stream));
         fetch_scalars(st, 1);
@@ -294,7 +308,9 @@ void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph)
     check_cuda(cudaMemsetAsync(pcmax, 0, (size_t)d * 4, st->stream));
     uint32_t *pidpc = d < (1u << 24) ? slot<uint32_t>(st, S_PIDPC, z) : nullptr;
     k_phrase_finalize<<<grid_for(z, 256), 256, 0, st->stream>>>(dT, n, ph.D, z, W, slot_of, tdense, pid, pidpc,
-                                                                occ, pcmin, pcmax);
+                                                                occ, pcmin, pcmax, xsep,
+                                                                bt ? bt->ptid : nullptr,
+                                                                bt ? bt->lastb : nullptr);
     ph.pidpc = pidpc;
     after_launch(st);
     // dictionary offsets (64-bit scan, checked against 2^32)

@@ -236,6 +236,239 @@ uint32_t run_trigger_scan(Storage *st, const uint8_t *dT, uint32_t n, int W, int
 }
 
 // ---------------------------------------------------------------------
+// Batched trigger scan over a padded buffer X of many texts: text t at
+// xstart[t] followed by W sentinel bytes (1).  Per text the windows are
+// those of its own scan (start s >= 1 inside the text, s+W-1 < n_t), and
+// the text's forced final trigger is the all-sentinel window right after it.
+// Both tests read only X: the W+1 bytes X[s-1 .. s+W-1] hold no sentinel
+// for an ordinary window, and exactly W (all but X[s-1]) for the forced one.
+// The first-window rule compares with the first window of the window's own
+// text, whose index is the number of text starts up to s, minus one.
+// ---------------------------------------------------------------------
+struct BatchScanArgs {
+    const uint32_t *tile_text;   // [tiles] text starts before each tile
+    const uint64_t *fw;          // [k] first window of each text (packed, or fingerprint)
+    const uint32_t *xstart;      // [k] text starts in X
+};
+
+// First windows: packed big-endian bytes for W <= 8, else the fingerprint
+// used by the scan (both as computed by tile_triggers).
+__global__ void k_first_words(const uint8_t *X, const uint32_t *xstart, uint32_t k, int W, uint64_t *fw)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    const uint8_t *p = X + xstart[t];
+    uint64_t v = 0;
+    if (W <= 8) {
+        for (int i = 0; i < W; i++) v = (v << 8) | p[i];
+    } else {
+        for (int i = 0; i < W; i++) v = v * FP_BASE + p[i];
+    }
+    fw[t] = v;
+}
+
+// tile_text[b] = number of text starts below b * TS_TILE.
+__global__ void k_tile_text(const uint32_t *xstart, uint32_t k, uint32_t tiles, uint32_t *tile_text)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= tiles) return;
+    const uint32_t base = b * (uint32_t)TS_TILE;
+    uint32_t lo = 0, hi = k;        // first index with xstart >= base
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (xstart[mid] < base) lo = mid + 1; else hi = mid;
+    }
+    tile_text[b] = lo;
+}
+
+template <int WT, int PT>
+__device__ __forceinline__ uint32_t tile_triggers_batch(const ScanArgs &a, const BatchScanArgs &b, const uint8_t *s,
+                                                        uint32_t prevb, size_t base, uint32_t tcur, uint64_t fp_pow)
+{
+    constexpr int NB = TS_PER_THREAD + (WT > 0 ? WT : TS_MAXW) - 1;
+    constexpr int NV = (NB + 15) / 16;
+    const int W = WT > 0 ? WT : a.W;
+    const uint32_t P = PT > 0 ? (uint32_t)PT : (uint32_t)a.P;
+    const size_t s0 = base + (size_t)threadIdx.x * TS_PER_THREAD;
+    if (s0 >= a.n) return 0;
+
+    uint32_t w[NV * 4];
+    const uint8_t *src = s + (size_t)threadIdx.x * TS_PER_THREAD;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        uint4 q = *(const uint4 *)(src + v * 16);
+        w[v * 4 + 0] = q.x; w[v * 4 + 1] = q.y; w[v * 4 + 2] = q.z; w[v * 4 + 3] = q.w;
+    }
+    uint32_t h = 0, c1 = prevb == 1u;
+    {
+        uint32_t pw = 1, acc = 0;
+#pragma unroll
+        for (int i = (WT > 0 ? WT : TS_MAXW) - 1; i >= 0; i--) {
+            if (WT == 0 && i >= W) continue;
+            const uint32_t c = bget(w, i);
+            acc += c * pw;
+            c1 += c == 1u;
+            pw = (pw * 2u) % P;
+            if (WT == 0 || WT > 16) acc %= P;
+        }
+        h = acc % P;
+    }
+    uint64_t reg = 0, fp = 0;
+    if (WT > 0 && WT <= 8) {
+#pragma unroll
+        for (int i = 0; i < (WT > 0 ? WT : 1); i++) reg = (reg << 8) | bget(w, i);
+    } else {
+#pragma unroll
+        for (int i = 0; i < (WT > 0 ? WT : TS_MAXW); i++) {
+            if (WT == 0 && i >= W) break;
+            fp = fp * FP_BASE + bget(w, i);
+        }
+    }
+    const uint64_t regmask = (WT > 0 && WT < 8) ? ((1ull << (8 * (WT > 0 ? WT : 1))) - 1ull) : ~0ull;
+    uint64_t cur = tcur ? __ldg(b.fw + tcur - 1) : 0ull;
+
+    uint32_t mask = 0;
+#pragma unroll
+    for (int j = 0; j < TS_PER_THREAD; j++) {
+        const size_t sj = s0 + j;
+        const uint32_t pb = j ? bget(w, j - 1) : prevb, c = bget(w, j);
+        const bool inside = sj < a.n;
+        if (inside && pb == 1u && c != 1u) {          // a text starts at sj
+            tcur++;
+            cur = __ldg(b.fw + tcur - 1);
+        }
+        if (inside) {
+            bool hit = false;
+            if (c1 == 0) {
+                bool eq;
+                if (WT > 0 && WT <= 8) {
+                    eq = reg == cur;
+                } else {
+                    eq = false;
+                    if (fp == cur) {
+                        const uint8_t *f = a.T + __ldg(b.xstart + tcur - 1);
+                        eq = true;
+                        for (int i = 0; i < W; i++)
+                            if (s[sj - base + i] != __ldg(f + i)) { eq = false; break; }
+                    }
+                }
+                hit = h == 0 || eq;
+            } else {
+                hit = pb != 1u && c1 == (uint32_t)W;   // forced end of the text
+            }
+            if (hit) mask |= 1u << j;
+        }
+        if (j + 1 < TS_PER_THREAD) {
+            const uint32_t in = bget(w, j + W);
+            h = (2u * h + in + 256u * P - c * a.wW) % P;
+            c1 += (in == 1u) - (pb == 1u);
+            if (WT > 0 && WT <= 8) reg = ((reg << 8) | in) & regmask;
+            else fp = fp * FP_BASE - (uint64_t)c * fp_pow + in;
+        }
+    }
+    return mask;
+}
+
+template <int WT, int PT, bool WRITE>
+__global__ void __launch_bounds__(TS_THREADS) k_trigger_batch(ScanArgs a, BatchScanArgs b, uint32_t *counts,
+                                                              const uint32_t *offsets, uint32_t *D)
+{
+    __shared__ __align__(16) uint8_t s[TS_TILE + TS_MAXW + 64];
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_prev;
+    const int W = WT > 0 ? WT : a.W;
+    const size_t base = (size_t)blockIdx.x * TS_TILE;
+    const int halo16 = (W - 1 + 15) / 16 + 1;
+    stage_tile(a, s, base, halo16);
+    if (threadIdx.x == 0) s_prev = base ? __ldg(a.T + base - 1) : 1u;
+    __syncthreads();
+    // text starts among this thread's 16 positions -> text count before s0
+    const uint32_t o = threadIdx.x * TS_PER_THREAD;
+    const uint32_t prevb = threadIdx.x ? s[o - 1] : s_prev;
+    uint32_t nst = 0;
+    {
+        uint32_t pb = prevb;
+#pragma unroll
+        for (int j = 0; j < TS_PER_THREAD; j++) {
+            const uint32_t c = s[o + j];
+            nst += (base + o + j < a.n && pb == 1u && c != 1u) ? 1u : 0u;
+            pb = c;
+        }
+    }
+    uint32_t tot;
+    const uint32_t ex_st = block_excl_scan<uint32_t, OpAdd>(nst, tot, OpAdd(), s_warp);
+    const uint32_t tcur = __ldg(b.tile_text + blockIdx.x) + ex_st;
+    __syncthreads();
+    uint64_t fp_pow = 1;
+    for (int i = 0; i < W; i++) fp_pow *= FP_BASE;
+    uint32_t mask = tile_triggers_batch<WT, PT>(a, b, s, prevb, base, tcur, fp_pow);
+    uint32_t cnt = __popc(mask), total;
+    uint32_t ex = block_excl_scan<uint32_t, OpAdd>(cnt, total, OpAdd(), s_warp);
+    if (!WRITE) {
+        if (threadIdx.x == 0) counts[blockIdx.x] = total;
+        return;
+    }
+    uint32_t out = offsets[blockIdx.x] + ex;
+    const uint32_t s0 = (uint32_t)(base + o);
+    while (mask) {
+        int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        D[out++] = s0 + (uint32_t)j + (uint32_t)W - 1u;
+    }
+}
+
+template <int WT, int PT>
+static uint32_t launch_pair_batch(Storage *st, const ScanArgs &a, const BatchScanArgs &b, unsigned blocks,
+                                  uint32_t *counts, uint32_t *&D)
+{
+    probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
+    k_trigger_batch<WT, PT, false><<<blocks, TS_THREADS, 0, st->stream>>>(a, b, counts, nullptr, nullptr);
+    probe_end(st, GBWT_PROBE_TRIGGER_SCAN, a.n);
+    after_launch(st);
+    uint32_t *tot = (uint32_t *)st->d_scalars;
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, blocks, LoadArr<uint32_t>{counts}, StoreArr<uint32_t>{counts}, false, tot);
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 1, a.flags, 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars, st->d_scalars, 8, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    const uint32_t flags = (uint32_t)st->h_scalars[1];
+    if (flags & ERR_BAD_BYTE) throw Error{GBWT_BAD_PARAMETER};
+    if (flags & ERR_SMALL_RANGE) throw Error{GBWT_UNSUPPORTED_INPUT};
+    const uint32_t c = (uint32_t)(st->h_scalars[0] & 0xFFFFFFFFu);
+    D = slot<uint32_t>(st, S_D, (size_t)c + 1);
+    probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
+    k_trigger_batch<WT, PT, true><<<blocks, TS_THREADS, 0, st->stream>>>(a, b, nullptr, counts, D);
+    probe_end(st, GBWT_PROBE_TRIGGER_SCAN, (uint64_t)a.n + 4ull * c);
+    after_launch(st);
+    return c;
+}
+
+uint32_t run_trigger_scan_batch(Storage *st, const uint8_t *dX, uint32_t N, int W, int P, const uint32_t *xstart,
+                                uint32_t k, uint32_t *&D)
+{
+    ScanArgs a;
+    a.T = dX; a.n = N; a.W = W; a.P = P;
+    uint32_t wW = 1;
+    for (int i = 0; i < W; i++) wW = (wW * 2u) % (uint32_t)P;
+    a.wW = wW;
+    a.hi = 254u;             // bytes were checked when X was built
+    a.flags = st->d_flags;
+    const unsigned blocks = grid_for(N, TS_TILE);
+    uint32_t *counts = slot<uint32_t>(st, S_TMP0, blocks + 1);
+    uint32_t *tile_text = slot<uint32_t>(st, S_TMP1, blocks);
+    uint64_t *fw = slot<uint64_t>(st, S_TMP2, k);
+    k_first_words<<<grid_for(k, 256), 256, 0, st->stream>>>(dX, xstart, k, W, fw);
+    after_launch(st);
+    k_tile_text<<<grid_for(blocks, 256), 256, 0, st->stream>>>(xstart, k, blocks, tile_text);
+    after_launch(st);
+    BatchScanArgs b{tile_text, fw, xstart};
+    if (W == 5 && P == 16) return launch_pair_batch<5, 16>(st, a, b, blocks, counts, D);
+    if (W == 5 && P == 23) return launch_pair_batch<5, 23>(st, a, b, blocks, counts, D);
+    if (W == 35 && P == 81) return launch_pair_batch<35, 81>(st, a, b, blocks, counts, D);
+    return launch_pair_batch<0, 0>(st, a, b, blocks, counts, D);
+}
+
+// ---------------------------------------------------------------------
 // Allocation-free trigger scan.
 //
 // Some callers cannot allocate device memory themselves: code running

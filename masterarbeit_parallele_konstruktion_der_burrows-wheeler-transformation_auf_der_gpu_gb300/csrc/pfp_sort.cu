@@ -39,6 +39,11 @@ struct ParseRem {
     uint32_t n;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return n - x; }
 };
+// A batch of parses laid end to end: a suffix ends with its own text.
+struct BatchParseRem {
+    const uint32_t *ptid, *zend;
+    __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return zend[ptid[x]] - x; }
+};
 
 __global__ void k_iota(uint32_t *v, uint32_t n)
 {
@@ -734,6 +739,33 @@ void run_parse_sa(Storage *st, Phrases &ph, DictOrder &dord, ParseOrder &pord)
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
     pord.rounds = prefix_doubling(st, z, lb + bits_for(ph.d - 1), 2u, ParseRem{z}, pord.isa, pord.sa);
+}
+
+// Batch: the second symbol of a key is 0 when phrase i ends its text.
+__global__ void k_parse_keys_batch(const uint32_t *pid, const uint32_t *lexrank, const uint32_t *ptid, uint32_t z,
+                                   int lb, uint64_t *keys)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= z) return;
+    uint64_t a = lexrank[pid[i]];
+    uint64_t b = (i + 1 < z && ptid[i + 1] == ptid[i]) ? (uint64_t)lexrank[pid[i + 1]] + 1u : 0u;
+    keys[i] = (a << lb) | b;
+}
+
+// Suffix array over all texts' parses at once.  Suffixes of different texts
+// may be equal strings and then share a rank; the order restricted to one
+// text is that text's own parse suffix array.
+void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchText &bt, ParseOrder &pord)
+{
+    const uint32_t z = ph.z;
+    uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
+    const int lb = bits_for(ph.d);
+    k_parse_keys_batch<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bt.ptid, z, lb, keys);
+    after_launch(st);
+    pord.isa = slot<uint32_t>(st, S_PISA, z);
+    pord.sa = slot<uint32_t>(st, S_PSA, z);
+    pord.rounds = prefix_doubling(st, z, lb + bits_for(ph.d - 1), 2u, BatchParseRem{bt.ptid, bt.zend}, pord.isa,
+                                  pord.sa);
 }
 
 }  // namespace gbwt

@@ -120,3 +120,36 @@ def config3_text(scale: float = 1.0) -> np.ndarray:
 def random_text(n: int, alphabet: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return rng.integers(2, 2 + alphabet, size=n).astype(np.uint8)
+
+
+def batch_lengths(count: int = 4096, median: float = 64 * 1024, sigma: float = 1.2, lo: int = 4 * 1024,
+                  hi: int = 16 * MiB, seed: int = 4) -> np.ndarray:
+    """Log-normal text lengths (median, sigma), clipped to [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.clip(np.rint(rng.lognormal(np.log(median), sigma, size=count)), lo, hi).astype(np.int64)
+
+
+def batch_texts(count: int = 4096, scale: float = 1.0, seed: int = 4, sub_rate: float = 1e-3):
+    """Batched workload: `count` independent texts with log-normal lengths
+    (median 64 KiB * scale, sigma 1.2, clipped to [4 KiB, 16 MiB] * scale),
+    each 8..64 mutated copies of its own uniform ACGT base.  Returns
+    (concatenated bytes, int64 offsets[count + 1])."""
+    lens = batch_lengths(count, 64 * 1024 * scale, 1.2, max(1, int(4 * 1024 * scale)), max(1, int(16 * MiB * scale)),
+                         seed)
+    rng = np.random.default_rng(seed + 1)
+    parts = []
+    for ln in lens.tolist():
+        copies = int(rng.integers(8, 65))
+        base = DNA[rng.integers(0, 4, size=max(1, ln // copies))]
+        t = np.tile(base, copies)[:ln]
+        if len(t) < ln:
+            t = np.concatenate([t, DNA[rng.integers(0, 4, size=ln - len(t))]])
+        parts.append(_substitute(rng, t, sub_rate))
+    offsets = np.zeros(count + 1, dtype=np.int64)
+    np.cumsum(lens, out=offsets[1:])
+    return np.concatenate(parts), offsets
+
+
+def config4_texts(scale: float = 1.0):
+    """4096 texts, about 512 MiB in total (seed 4)."""
+    return batch_texts(4096, scale, seed=4)

@@ -76,3 +76,20 @@ def test_variant_names(pkg):
 def test_cli_built(pkg):
     cli = os.path.join(os.path.dirname(pkg.LIB_PATH), "gbwt_pfp")
     assert os.access(cli, os.X_OK)
+
+
+def test_batch_workload_shape(wl):
+    lens = wl.batch_lengths(4096)
+    assert lens.min() >= 4 * 1024 and lens.max() <= 16 * 1024 * 1024
+    assert 400 * 2**20 < lens.sum() < 640 * 2**20          # about 512 MiB
+    assert abs(np.median(lens) - 64 * 1024) < 8 * 1024
+    c, o = wl.batch_texts(8, scale=1 / 64, seed=5)
+    c2, o2 = wl.batch_texts(8, scale=1 / 64, seed=5)
+    assert np.array_equal(c, c2) and np.array_equal(o, o2)
+    assert o[0] == 0 and o[-1] == len(c) and c.min() >= 2 and c.max() <= 5
+
+
+def test_batch_wrapper_validates_before_calling(pkg):
+    st = object.__new__(pkg.Storage)      # no device storage: validation must fail first
+    with pytest.raises(ValueError):
+        pkg.Storage.pfp_bwt_batch_into(st, np.zeros(4, np.uint8), np.array([0, 8]), np.zeros(8, np.uint8))
