@@ -94,74 +94,109 @@ struct StoreTid {
     }
 };
 
-// Emission slots: k empty parse suffixes (slot t stands for the last phrase
-// of text t), then the parse suffix array; slot of suffix x stands for the
-// phrase before it, none when x starts its text.
+// ---------------------------------------------------------------------
+// Output elements.  Texts are grouped into segments of consecutive texts
+// (a segment closes once it holds SEG_MIN elements), each padded to whole
+// radix tiles.  Every text position of text t becomes one key
+//   (t - first text of its segment, dictionary group, recoded byte)
+// written at its segment position in text-major, parse-suffix order; one
+// segmented stable radix sort then leaves each text's elements in its BWT
+// order, padding (all-ones keys) at the segment ends.
+// ---------------------------------------------------------------------
+constexpr uint32_t SEG_MIN = 8u * RS_TILE;
+
+struct BatchLayout {
+    uint32_t k = 0;                 // non-empty texts
+    uint64_t total = 0, N = 0;      // text bytes; bytes of X
+    uint32_t tiles = 0;             // padded element tiles
+    uint32_t max_local = 1;         // most texts in one segment
+    // word offsets into h_meta / the device copy
+    size_t o_xstart = 0, o_ioff = 0, o_pshift = 0, o_tloc = 0, o_tseg = 0, o_tout = 0, words = 0;
+};
+
+// Text-major order of the parse suffix array: stable partition by text.
+__global__ void k_text_keys(const uint32_t *psa, const uint32_t *ptid, uint32_t z, uint32_t *keys, uint32_t *vals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= z) return;
+    const uint32_t x = psa[i];
+    keys[i] = ptid[x];
+    vals[i] = x;
+}
+
+// Slots, text-major: text t owns slots [zs_t + t, zend_t + t] -- first its
+// empty parse suffix (standing for its last phrase, K:787-807), then its
+// suffixes in order (suffix x stands for phrase x-1; none when x starts the
+// text).  Thread i handles the suffix at text-major position i.
 struct BatchEmit {
     const uint32_t *psa, *pid, *pidpc, *D, *ptid, *zend, *dlen, *doff;
     const uint8_t *X, *lastb;
-    uint32_t k, z;
+    uint32_t z;
     int W;
+    __device__ __forceinline__ void fill(uint32_t occ, uint32_t s, uint32_t *emq, uint32_t *emt, uint8_t *emp,
+                                         uint32_t *ecnt) const
+    {
+        uint32_t q, prev;
+        if (pidpc) {
+            const uint32_t v = pidpc[occ];
+            q = v >> 8;
+            prev = v & 0xFFu;
+        } else {
+            q = pid[occ];
+            const bool first = occ == 0 || X[D[occ - 1]] == 1;
+            prev = first ? lastb[ptid[occ]] : X[D[occ - 1] - (uint32_t)W];
+        }
+        emq[s] = doff[q];
+        emt[s] = ptid[occ];
+        emp[s] = (uint8_t)prev;
+        ecnt[s] = dlen[q] - (uint32_t)W;
+    }
 };
 
 __global__ void k_bemit_prep(BatchEmit e, uint32_t *emq, uint32_t *emt, uint8_t *emp, uint32_t *ecnt)
 {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= e.k + e.z) return;
-    uint32_t occ;
-    if (s < e.k) {
-        occ = e.zend[s] - 1u;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e.z) return;
+    const uint32_t x = e.psa[i], t = e.ptid[x];
+    const uint32_t zs = t ? e.zend[t - 1] : 0u;
+    const uint32_t s = i + t + 1u;
+    if (i == zs) e.fill(e.zend[t] - 1u, s - 1u, emq, emt, emp, ecnt);
+    if (x == zs) {
+        emq[s] = 0; emt[s] = t; emp[s] = 0; ecnt[s] = 0;
     } else {
-        const uint32_t x = e.psa[s - e.k];
-        if (x == 0 || e.ptid[x - 1] != e.ptid[x]) {
-            emq[s] = 0; emt[s] = 0; emp[s] = 0; ecnt[s] = 0;
-            return;
-        }
-        occ = x - 1u;
+        e.fill(x - 1u, s, emq, emt, emp, ecnt);
     }
-    uint32_t q, prev;
-    if (e.pidpc) {
-        const uint32_t v = e.pidpc[occ];
-        q = v >> 8;
-        prev = v & 0xFFu;
-    } else {
-        q = e.pid[occ];
-        const bool first = occ == 0 || e.X[e.D[occ - 1]] == 1;
-        prev = first ? e.lastb[e.ptid[occ]] : e.X[e.D[occ - 1] - (uint32_t)e.W];
-    }
-    emq[s] = e.doff[q];
-    emt[s] = e.ptid[occ];
-    emp[s] = (uint8_t)prev;
-    ecnt[s] = e.dlen[q] - (uint32_t)e.W;
 }
 
 // 256 slots per CTA; consecutive threads write consecutive elements.
 constexpr int BE_T = 256;
+template <typename E>
 __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff, const uint32_t *emq,
-                                                const uint32_t *emt, const uint8_t *emp, const uint32_t *grp_of,
-                                                const uint8_t *dict, int gb, uint64_t *elem, uint32_t cap,
+                                                const uint32_t *emt, const uint8_t *emp, const uint32_t *pshift,
+                                                const uint32_t *tloc, const uint32_t *grp_of, const uint8_t *dict,
+                                                const uint8_t *enc, int gbb, int bb, E *elem, uint32_t cap,
                                                 uint32_t *flags)
 {
     __shared__ uint32_t s_off[BE_T + 1];
     __shared__ uint32_t s_base[BE_T];
-    __shared__ uint64_t s_hi[BE_T];
+    __shared__ uint32_t s_shift[BE_T];
+    __shared__ E s_hi[BE_T];
     __shared__ uint8_t s_prev[BE_T];
+    __shared__ uint8_t s_enc[256];
     const uint32_t t0 = blockIdx.x * BE_T;
     const uint32_t tn = min((uint32_t)BE_T, S - t0);
+    s_enc[threadIdx.x] = enc[threadIdx.x];          // blockDim == 256
     if (threadIdx.x < tn) {
-        const uint32_t t = t0 + threadIdx.x;
-        s_off[threadIdx.x] = eoff[t];
-        s_base[threadIdx.x] = emq[t];
-        s_hi[threadIdx.x] = (uint64_t)emt[t] << gb;
-        s_prev[threadIdx.x] = emp[t];
+        const uint32_t s = t0 + threadIdx.x, t = emt[s];
+        s_off[threadIdx.x] = eoff[s];
+        s_base[threadIdx.x] = emq[s];
+        s_shift[threadIdx.x] = pshift[t];
+        s_hi[threadIdx.x] = gbb < (int)(8 * sizeof(E)) ? (E)tloc[t] << gbb : (E)0;
+        s_prev[threadIdx.x] = emp[s];
     }
     if (threadIdx.x == 0) s_off[tn] = eoff[t0 + tn];
     __syncthreads();
     const uint32_t o0 = s_off[0], cnt = s_off[tn] - o0;
-    if ((uint64_t)o0 + cnt > cap) {
-        if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL);
-        return;
-    }
     for (uint32_t i = threadIdx.x; i < cnt; i += BE_T) {
         const uint32_t o = o0 + i;
         uint32_t lo = 0, hi = tn - 1u;            // last slot with s_off <= o
@@ -172,57 +207,134 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
         const uint32_t j = o - s_off[lo];
         const uint32_t pos = s_base[lo] + j;
         const uint32_t c = j ? dict[pos - 1] : s_prev[lo];
-        elem[o] = ((s_hi[lo] | grp_of[pos]) << 8) | c;
+        const uint32_t dst = o + s_shift[lo];
+        if (dst < cap) elem[dst] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
+        else atomicOr(flags, ERR_INTERNAL);
     }
 }
 
-// Output bytes = the low byte of the sorted elements, 16 per thread.
-__global__ void k_extract(const uint64_t *elem, uint32_t n, uint8_t *out)
+// Segment elements back to output bytes: tile b holds segment positions
+// [(b - first) * RS_TILE, +RS_TILE); tout[b] = {output base, real elements}.
+template <typename E>
+__global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, const uint8_t *dec, uint32_t bmask,
+                           uint8_t *out)
 {
-    const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * 16u;
-    if (i0 >= n) return;
-    if (i0 + 16u <= n && (((uintptr_t)(out + i0)) & 15u) == 0) {
-        uint8_t b[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) b[j] = (uint8_t)elem[i0 + j];
-        uint4 v;
-        memcpy(&v, b, 16);
-        *(uint4 *)(out + i0) = v;
-    } else {
-        for (uint32_t j = 0; j < 16 && i0 + j < n; j++) out[i0 + j] = (uint8_t)elem[i0 + j];
+    __shared__ uint8_t s_dec[256];
+    s_dec[threadIdx.x] = dec[threadIdx.x];          // blockDim == 256
+    __syncthreads();
+    const uint32_t b = blockIdx.x;
+    const uint2 sg = tseg[b], to = tout[b];
+    const uint32_t p0 = (b - sg.x) * (uint32_t)RS_TILE;
+    const size_t e0 = (size_t)b * RS_TILE;
+    for (uint32_t j = threadIdx.x; j < (uint32_t)RS_TILE; j += 256) {
+        const uint32_t p = p0 + j;
+        if (p < to.y) out[to.x + p] = s_dec[(uint32_t)elem[e0 + j] & bmask];
     }
 }
 
-// Texts with offsets[t] < offsets[t+1]; their layout in X.  Returns the
-// number of non-empty texts; h_meta receives xstart[k'+1] then ioff[k'].
-static uint32_t batch_layout(Storage *st, const int64_t *offsets, int32_t k, int W, uint64_t &total, uint64_t &N)
+// Host layout of a batch: the non-empty texts in X, and the segments.
+static BatchLayout batch_layout(Storage *st, const int64_t *offsets, int32_t k, int W)
 {
-    total = (uint64_t)offsets[k];
+    BatchLayout bl;
+    bl.total = (uint64_t)offsets[k];
     uint32_t kk = 0;
-    for (int32_t t = 0; t < k; t++) kk += offsets[t + 1] > offsets[t] ? 1u : 0u;
-    const size_t need = (size_t)2 * kk + 1;
-    if (st->h_meta_cap < need) {
+    uint64_t tiles = 0, seg_real = 0;
+    for (int32_t t = 0; t < k; t++) {
+        const uint64_t len = (uint64_t)(offsets[t + 1] - offsets[t]);
+        if (!len) continue;
+        kk++;
+        seg_real += len;
+        if (seg_real >= SEG_MIN) {
+            tiles += (seg_real + RS_TILE - 1) / RS_TILE;
+            seg_real = 0;
+        }
+    }
+    tiles += (seg_real + RS_TILE - 1) / RS_TILE;
+    if (tiles > 0xFFFFFFFFull / RS_TILE) throw Error{GBWT_UNSUPPORTED_INPUT};
+    bl.k = kk;
+    bl.tiles = (uint32_t)tiles;
+    bl.o_xstart = 0;
+    bl.o_ioff = kk + 1;
+    bl.o_pshift = bl.o_ioff + kk;
+    bl.o_tloc = bl.o_pshift + kk;
+    bl.o_tseg = (bl.o_tloc + kk + 1) & ~(size_t)1;      // 8-byte aligned uint2 arrays
+    bl.o_tout = bl.o_tseg + 2 * (size_t)bl.tiles;
+    bl.words = bl.o_tout + 2 * (size_t)bl.tiles;
+    if (st->h_meta_cap < bl.words) {
         if (st->h_meta) check_cuda(cudaFreeHost(st->h_meta));
         st->h_meta = nullptr;
         st->h_meta_cap = 0;
-        size_t cap = need + need / 4 + 1024;
+        const size_t cap = bl.words + bl.words / 4 + 1024;
         check_cuda(cudaHostAlloc(&st->h_meta, cap * sizeof(uint32_t), cudaHostAllocDefault));
         st->h_meta_cap = cap;
     }
-    uint32_t *xs = st->h_meta, *io = st->h_meta + kk + 1;
-    uint32_t i = 0;
-    uint64_t x = 0;
+    uint32_t *h = st->h_meta;
+    uint32_t *xs = h + bl.o_xstart, *io = h + bl.o_ioff, *ps = h + bl.o_pshift, *tl = h + bl.o_tloc;
+    uint32_t *tseg = h + bl.o_tseg, *tout = h + bl.o_tout;
+    uint32_t i = 0, seg_first_text = 0, tile = 0;
+    uint64_t x = 0, seg_obase = 0;
+    seg_real = 0;
+    auto close_segment = [&](uint32_t last_text) {
+        const uint32_t nt = (uint32_t)((seg_real + RS_TILE - 1) / RS_TILE);
+        for (uint32_t b = 0; b < nt; b++) {
+            tseg[2 * (tile + b)] = tile;
+            tseg[2 * (tile + b) + 1] = nt;
+            tout[2 * (tile + b)] = (uint32_t)seg_obase;
+            tout[2 * (tile + b) + 1] = (uint32_t)seg_real;
+        }
+        const uint32_t ntext = last_text - seg_first_text;
+        if (ntext > bl.max_local) bl.max_local = ntext;
+        // element position = output position + padding of earlier segments
+        const uint32_t shift = (uint32_t)((uint64_t)tile * RS_TILE - seg_obase);
+        for (uint32_t u = seg_first_text; u < last_text; u++) ps[u] = shift;
+        tile += nt;
+        seg_obase += seg_real;
+        seg_real = 0;
+        seg_first_text = last_text;
+    };
     for (int32_t t = 0; t < k; t++) {
         const uint64_t len = (uint64_t)(offsets[t + 1] - offsets[t]);
         if (!len) continue;
         xs[i] = (uint32_t)x;
         io[i] = (uint32_t)offsets[t];
+        tl[i] = i - seg_first_text;
         x += len + (uint64_t)W;
+        seg_real += len;
         i++;
+        if (seg_real >= SEG_MIN) close_segment(i);
     }
+    if (seg_real) close_segment(i);
     xs[kk] = (uint32_t)x;
-    N = x;
-    return kk;
+    bl.N = x;
+    return bl;
+}
+
+// Emission, segmented sort and extraction with E-bit keys.
+template <typename E>
+static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dmeta, uint32_t S,
+                         const uint32_t *eoff, const uint32_t *emq, const uint32_t *emt, const uint8_t *emp,
+                         const uint32_t *grp_of, const uint8_t *dict, const uint8_t *codes, int gb, int bb, int tlb,
+                         uint8_t *dOut)
+{
+    const uint32_t M = bl.tiles * (uint32_t)RS_TILE;
+    E *elem = slot<E>(st, S_ELEM0, M);
+    E *elem_alt = slot<E>(st, S_ELEM1, M);
+    check_cuda(cudaMemsetAsync(elem, 0xFF, (size_t)M * sizeof(E), st->stream));    // padding keys
+    k_bemit<E><<<grid_for(S, BE_T), BE_T, 0, st->stream>>>(S, eoff, emq, emt, emp, dmeta + bl.o_pshift,
+                                                           dmeta + bl.o_tloc, grp_of, dict, codes, gb + bb, bb, elem,
+                                                           M, st->d_flags);
+    after_launch(st);
+    const uint2 *tseg = (const uint2 *)(dmeta + bl.o_tseg);
+    // sort by (text, group) only: the byte rides along, and elements of one
+    // group keep their parse-suffix order
+    const int sb = tlb + gb;
+    uint32_t *nv = nullptr, *nv2 = nullptr;
+    if ((sb + 9) / 10 < (sb + 7) / 8) radix_sort<E, false, 10>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    stage_mark(st, 5);
+    k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,
+                                                    (1u << bb) - 1u, dOut);
+    after_launch(st);
 }
 
 int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t k, uint8_t *L, int W, int P,
@@ -241,14 +353,15 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     st->stage_times = (flags & GBWT_FLAG_STAGE_TIMES) != 0;
     if (total_i == 0) return 0;
     if (!T || !L) return GBWT_BAD_PARAMETER;
-    uint64_t total = 0, N = 0;
     // 32-bit positions inside, with room for the sentinel runs
     if ((uint64_t)total_i + (uint64_t)W * (uint64_t)k > (uint64_t)max_n) return GBWT_UNSUPPORTED_INPUT;
-    const uint32_t kk = batch_layout(st, offsets, k, W, total, N);
+    const BatchLayout bl = batch_layout(st, offsets, k, W);
+    const uint32_t kk = bl.k;
+    const uint64_t total = bl.total, N = bl.N;
 
-    uint32_t *meta = slot<uint32_t>(st, S_BMETA, (size_t)2 * kk + 1);
-    check_cuda(cudaMemcpyAsync(meta, st->h_meta, ((size_t)2 * kk + 1) * 4, cudaMemcpyHostToDevice, st->stream));
-    const uint32_t *xstart = meta, *ioff = meta + kk + 1;
+    uint32_t *meta = slot<uint32_t>(st, S_BMETA, bl.words);
+    check_cuda(cudaMemcpyAsync(meta, st->h_meta, bl.words * 4, cudaMemcpyHostToDevice, st->stream));
+    const uint32_t *xstart = meta + bl.o_xstart, *ioff = meta + bl.o_ioff;
     const uint8_t *dT;
     uint8_t *dOut;
     if (devptr) {
@@ -296,19 +409,43 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     DictOrder dord;
     run_dict_sort(st, ph, W, small, dord);
     st->stats.dict_rounds = dord.rounds;
+    // byte codes of the dictionary's alphabet (pinned, written by the sort):
+    // code 1 is the sentinel, text bytes have codes 2.. -> output codes 0..
+    uint8_t *hcodes = (uint8_t *)(st->h_scalars + 16);
+    uint8_t *hpack = (uint8_t *)(st->h_scalars + 80);        // enc[256] dec[256]
+    uint32_t sigma = 0;
+    for (int c = 0; c < 256; c++) {
+        hpack[c] = 0;
+        hpack[256 + c] = 0;
+    }
+    for (int c = 2; c < 256; c++)
+        if (hcodes[c]) {
+            hpack[c] = (uint8_t)(hcodes[c] - 2);
+            hpack[256 + hcodes[c] - 2] = (uint8_t)c;
+            sigma++;
+        }
+    uint8_t *codes = slot<uint8_t>(st, S_BCODE, 512);
+    check_cuda(cudaMemcpyAsync(codes, hpack, 512, cudaMemcpyHostToDevice, st->stream));
     stage_mark(st, 2);
 
     ParseOrder pord;
     run_parse_sa_batch(st, ph, dord, bt, pord);
     st->stats.parse_rounds = pord.rounds;
+    // text-major order of the parse suffix array (stable: each text keeps its order)
+    uint32_t *tkey = slot<uint32_t>(st, S_KEY0, z), *tkey2 = slot<uint32_t>(st, S_KEY1, z);
+    uint32_t *tval = slot<uint32_t>(st, S_VAL0, z), *tval2 = slot<uint32_t>(st, S_VAL1, z);
+    k_text_keys<<<grid_for(z, 256), 256, 0, st->stream>>>(pord.sa, ptid, z, tkey, tval);
+    after_launch(st);
+    radix_sort<uint32_t, true>(st, tkey, tkey2, tval, tval2, z, 0, bits_for(kk - 1u));
+    const uint32_t *psa_tm = tval;
     stage_mark(st, 3);
 
     uint32_t *grp_of = nullptr;
     const uint32_t G = run_group_index(st, ph, dord, W, grp_of);
     if (G == 0) throw Error{GBWT_INTERNAL_ERROR};
     st->stats.s = G;
-    const int tb = bits_for(kk - 1u), gb = bits_for(G - 1u);
-    if (8 + tb + gb > 64) throw Error{GBWT_UNSUPPORTED_INPUT};
+    const int tlb = bits_for(bl.max_local - 1u), gb = bits_for(G - 1u), bb = bits_for(sigma ? sigma - 1u : 0u);
+    if (tlb + gb + bb > 64) throw Error{GBWT_UNSUPPORTED_INPUT};
     stage_mark(st, 4);
 
     const uint32_t S = kk + z;
@@ -316,24 +453,18 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     uint32_t *emt = slot<uint32_t>(st, S_TMP1, S);
     uint8_t *emp = slot<uint8_t>(st, S_TMP2, S);
     uint32_t *ecnt = slot<uint32_t>(st, S_GCOUNT, (size_t)S + 1);
-    BatchEmit e{pord.sa, ph.pid, ph.pidpc, ph.D, ptid, zend, ph.dlen, ph.doff, X, lastb, kk, z, W};
-    k_bemit_prep<<<grid_for(S, 256), 256, 0, st->stream>>>(e, emq, emt, emp, ecnt);
+    BatchEmit e{psa_tm, ph.pid, ph.pidpc, ph.D, ptid, zend, ph.dlen, ph.doff, X, lastb, z, W};
+    k_bemit_prep<<<grid_for(z, 256), 256, 0, st->stream>>>(e, emq, emt, emp, ecnt);
     after_launch(st);
     device_scan<uint32_t, OpAdd>(st, S, LoadArr<uint32_t>{ecnt}, StoreArr<uint32_t>{ecnt}, false, ecnt + S);
     check_cuda(cudaMemcpyAsync(st->d_scalars, ecnt + S, 4, cudaMemcpyDeviceToDevice, st->stream));
     fetch_scalars(st, 1);
     if ((uint32_t)st->h_scalars[0] != (uint32_t)total) throw Error{GBWT_INTERNAL_ERROR};
-    const uint32_t M = (uint32_t)total;
-    uint64_t *elem = slot<uint64_t>(st, S_ELEM0, M);
-    uint64_t *elem_alt = slot<uint64_t>(st, S_ELEM1, M);
-    k_bemit<<<grid_for(S, BE_T), BE_T, 0, st->stream>>>(S, ecnt, emq, emt, emp, grp_of, ph.dict, gb, elem, M,
-                                                        st->d_flags);
-    after_launch(st);
-    uint32_t *nv = nullptr, *nv2 = nullptr;
-    radix_sort<uint64_t, false, 8>(st, elem, elem_alt, nv, nv2, M, 8, 8 + tb + gb);
-    stage_mark(st, 5);
-    k_extract<<<grid_for(M, 256 * 16), 256, 0, st->stream>>>(elem, M, dOut);
-    after_launch(st);
+    st->stats.mixed_elems = (int64_t)bl.tiles * RS_TILE;     // padded element count
+    if (tlb + gb + bb <= 32)
+        batch_output<uint32_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut);
+    else
+        batch_output<uint64_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut);
     stage_mark(st, 6);
     if (!devptr) check_cuda(cudaMemcpyAsync(L, dOut, (size_t)total, cudaMemcpyDeviceToHost, st->stream));
     check_cuda(cudaMemcpyAsync(st->h_scalars + 8, st->d_flags, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost,

@@ -189,10 +189,22 @@ __device__ __forceinline__ uint32_t rs_digit(K k, int shift, uint32_t mask)
     return (uint32_t)(k >> shift) & mask;
 }
 
+// Histogram slot of digit d for tile b.  Unsegmented: digit-major over all
+// tiles.  Segmented (tseg[b] = {first tile, tiles} of b's segment, every
+// segment a whole number of tiles): segment-major, then digit-major inside
+// the segment, so one exclusive scan gives every tile its offsets inside its
+// own segment and each pass sorts the segments independently.
+__device__ __forceinline__ size_t rs_hist_index(const uint2 *tseg, uint32_t b, uint32_t d, uint32_t num_tiles, int D)
+{
+    if (!tseg) return (size_t)d * num_tiles + b;
+    const uint2 q = tseg[b];
+    return (size_t)q.x * D + (size_t)d * q.y + (b - q.x);
+}
+
 template <typename K, int BITS>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__ keys, uint32_t n, int shift,
                                                            uint32_t mask, uint32_t *__restrict__ tile_hist,
-                                                           uint32_t num_tiles)
+                                                           uint32_t num_tiles, const uint2 *__restrict__ tseg)
 {
     constexpr int D = 1 << BITS;
     __shared__ uint32_t h[D];
@@ -208,7 +220,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__
         if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < D; d += RS_THREADS) tile_hist[(size_t)d * num_tiles + blockIdx.x] = h[d];
+    for (int d = threadIdx.x; d < D; d += RS_THREADS) tile_hist[rs_hist_index(tseg, blockIdx.x, d, num_tiles, D)] = h[d];
 }
 
 template <typename K, bool HAS_VAL, int BITS>
@@ -223,7 +235,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
                                                              const uint32_t *__restrict__ vin,
                                                              uint32_t *__restrict__ vout, uint32_t n, int shift,
                                                              uint32_t mask, const uint32_t *__restrict__ tile_off,
-                                                             uint32_t num_tiles)
+                                                             uint32_t num_tiles, const uint2 *__restrict__ tseg)
 {
     constexpr int D = 1 << BITS;
     constexpr int DPT = D / RS_THREADS;       // digits per thread in the per-digit phase
@@ -293,7 +305,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
             const uint32_t d = threadIdx.x * DPT + e;
             s_dstart[d] = ex;
             ex += cnt[e];
-            s_goff[d] = tile_off[(size_t)d * num_tiles + blockIdx.x];
+            s_goff[d] = tile_off[rs_hist_index(tseg, blockIdx.x, d, num_tiles, D)];
         }
     }
     __syncthreads();
@@ -319,10 +331,11 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
 // Sorts (keys, vals) stably by bits [begin_bit, end_bit) with BITS-bit digits
 // (8: 256 buckets; 10: 1024 buckets, fewer passes for 17..20-bit keys).  On
 // return `keys` and `vals` point at the sorted data (the *_alt buffers hold
-// garbage).
+// garbage).  With `tseg` (see rs_hist_index; n a multiple of RS_TILE) every
+// segment is sorted on its own.
 template <typename K, bool HAS_VAL, int BITS = 8>
 void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *&vals_alt, uint32_t n,
-                int begin_bit, int end_bit)
+                int begin_bit, int end_bit, const uint2 *tseg = nullptr)
 {
     static_assert((1 << BITS) % RS_THREADS == 0, "digit count must be a multiple of the CTA size");
     if (n <= 1 || end_bit <= begin_bit) return;
@@ -339,12 +352,13 @@ void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *
     for (int shift = begin_bit; shift < end_bit; shift += BITS) {
         int bits = end_bit - shift < BITS ? end_bit - shift : BITS;
         uint32_t mask = (1u << bits) - 1u;
-        k_rs_upsweep<K, BITS><<<num_tiles, RS_THREADS, 0, st->stream>>>(keys, n, shift, mask, hist, num_tiles);
+        k_rs_upsweep<K, BITS><<<num_tiles, RS_THREADS, 0, st->stream>>>(keys, n, shift, mask, hist, num_tiles, tseg);
         after_launch(st);
         scan_array_excl<uint32_t, OpAdd>(st, hist, D * num_tiles, 0);
         probe_begin(st, GBWT_PROBE_RADIX_SCATTER);
         k_rs_downsweep<K, HAS_VAL, BITS><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt,
-                                                                                      n, shift, mask, hist, num_tiles);
+                                                                                      n, shift, mask, hist, num_tiles,
+                                                                                      tseg);
         probe_end(st, GBWT_PROBE_RADIX_SCATTER, (uint64_t)n * 2 * (sizeof(K) + (HAS_VAL ? 4 : 0)));
         after_launch(st);
         K *t = keys; keys = keys_alt; keys_alt = t;

@@ -3,6 +3,8 @@ benchmark workloads; the command profilers (ncu) are pointed at.
 
   python -m <package>.profile_run --workload config2 --iters 1
   python -m <package>.profile_run --workload config2 --scale 0.125 --iters 2
+  python -m <package>.profile_run --workload config4 --iters 3            # batched
+  python -m <package>.profile_run --workload config4 --per-text --iters 1 # one text per call
 
 Prints one JSON line with the pipeline counts and per-stage times of the
 last iteration.  Exits non-zero if the BWT is not a permutation of the text.
@@ -20,7 +22,8 @@ PKG = os.path.basename(os.path.dirname(os.path.abspath(__file__)))
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--per-text", action="store_true", help="config4: one call per text instead of one batch")
     ap.add_argument("--scale", type=float, default=1.0, help="base length scale of the workload")
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--W", type=int, default=None)
@@ -32,6 +35,8 @@ def main(argv=None) -> int:
 
     pkg = importlib.import_module(PKG)
     wl = importlib.import_module(PKG + ".workloads")
+    if args.workload == "config4":
+        return run_batched(args, pkg, wl)
     text = getattr(wl, args.workload + "_text")(args.scale)
     W = args.W or 5
     P = args.P or (23 if args.workload == "config3" else 16)
@@ -49,6 +54,45 @@ def main(argv=None) -> int:
         print("profile_run: output is not a permutation of the text", file=sys.stderr)
         return 1
     stats.update({"workload": args.workload, "scale": args.scale, "n": n, "W": W, "P": P, "small": args.small})
+    print(json.dumps(stats))
+    return 0
+
+
+def run_batched(args, pkg, wl) -> int:
+    import numpy as np
+    import torch
+
+    concat, offsets = wl.config4_texts(args.scale)
+    W, P = args.W or 5, args.P or 16
+    n = len(concat)
+    dt = torch.from_numpy(concat).cuda()
+    do = torch.empty_like(dt)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    with pkg.Storage(n) as st:
+        st.set_stream(stream.cuda_stream)
+        ms = []
+        for i in range(args.iters):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if args.per_text:
+                for t in range(len(offsets) - 1):
+                    a, b = int(offsets[t]), int(offsets[t + 1])
+                    st.pfp_bwt_device(dt.data_ptr() + a, do.data_ptr() + a, b - a, W, P, args.small)
+            else:
+                st.pfp_bwt_batch_device(dt.data_ptr(), offsets, do.data_ptr(), W, P, args.small,
+                                        stage_times=(i == args.iters - 1))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        stats = st.stats()
+    out = do.cpu().numpy()
+    if not np.array_equal(np.bincount(out, minlength=256), np.bincount(concat, minlength=256)):
+        print("profile_run: output is not a permutation of the texts", file=sys.stderr)
+        return 1
+    stats.update({"workload": "config4", "per_text": args.per_text, "scale": args.scale, "n": n,
+                  "texts": len(offsets) - 1, "W": W, "P": P, "ms": [round(x, 3) for x in ms],
+                  "MBps_last": round(n / (ms[-1] / 1000) / 1e6, 1)})
     print(json.dumps(stats))
     return 0
 
