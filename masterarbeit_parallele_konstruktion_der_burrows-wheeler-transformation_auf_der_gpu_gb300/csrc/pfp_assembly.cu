@@ -41,52 +41,67 @@ __device__ __forceinline__ uint32_t pc_code(const uint8_t *dict, const uint32_t 
     return pcmin[q] == pcmax[q] ? pcmin[q] : PC_VAR;
 }
 
-// Pass 1 over the dictionary order: S elements, group index, block lengths.
-struct LoadSHead {
-    const uint32_t *sa, *isa;
-    PosInfo pi;
-    uint32_t W;
-    __device__ __forceinline__ uint32_t operator()(size_t t) const
-    {
-        uint32_t x = sa[t], q, off, rem;
-        pi.get(x, q, off, rem);
-        return (rem > W && isa[x] == (uint32_t)t) ? 1u : 0u;
-    }
+// S groups (equal phrase suffixes longer than W) in dictionary order.  The
+// passes run over dictionary positions x in storage order, so the phrase
+// tables are read almost sequentially: (1) mark the sorted position isa[x]
+// of every long suffix's group head, (2) scan the marks into group numbers,
+// (3) read each position's group back through isa[x].
+__global__ void k_mark_sheads(uint32_t N, PosInfo pi, uint32_t W, const uint32_t *isa, uint8_t *mark)
+{
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    uint32_t q, off, rem;
+    pi.get(x, q, off, rem);
+    if (rem > W) mark[isa[x]] = 1;
+}
+struct LoadMark {
+    const uint8_t *m;
+    __device__ __forceinline__ uint32_t operator()(size_t t) const { return m[t]; }
 };
-struct StoreSGroup {
-    const uint32_t *sa;
-    PosInfo pi;
-    uint32_t W;
-    const uint8_t *dict;
-    const uint32_t *occ, *pcmin, *pcmax;
-    uint32_t *gcount;
-    uint16_t *gchar;
-    uint32_t *grp_of;
+struct StoreGid {
+    const uint8_t *m;
+    uint32_t *gid;
     __device__ __forceinline__ void operator()(size_t t, uint32_t inc, uint32_t v) const
     {
-        uint32_t x = sa[t], q, off, rem;
-        pi.get(x, q, off, rem);
-        if (rem <= W) return;
-        const uint32_t g = inc - 1u;
-        grp_of[x] = g;
-        atomicAdd(gcount + g, occ[q]);
-        if (v) gchar[g] = (uint16_t)pc_code(dict, pcmin, pcmax, x, q, off);
+        if (v) gid[t] = inc - 1u;
     }
 };
 
-// Group index only (the batched assembly counts per text, not per group).
-struct StoreGroupOnly {
-    const uint32_t *sa;
-    PosInfo pi;
-    uint32_t W;
-    uint32_t *grp_of;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t inc, uint32_t) const
-    {
-        uint32_t x = sa[t], q, off, rem;
-        pi.get(x, q, off, rem);
-        if (rem > W) grp_of[x] = inc - 1u;
+// Group of every long suffix; with `gcount` also the block lengths (sum of
+// the phrases' occurrence counts) and one preceding-byte code per group
+// (any member's: the mixed test compares every member with it).
+__global__ void k_group_of(uint32_t N, PosInfo pi, uint32_t W, const uint32_t *isa, const uint32_t *gid,
+                           uint32_t *grp_of, const uint8_t *dict, const uint32_t *occ, const uint32_t *pcmin,
+                           const uint32_t *pcmax, uint32_t *gcount, uint16_t *gchar)
+{
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    uint32_t q, off, rem;
+    pi.get(x, q, off, rem);
+    if (rem <= W) return;
+    const uint32_t g = gid[isa[x]];
+    grp_of[x] = g;
+    if (gcount) {
+        atomicAdd(gcount + g, occ[q]);
+        gchar[g] = (uint16_t)pc_code(dict, pcmin, pcmax, x, q, off);
     }
-};
+}
+
+// Passes (1)-(2); returns the number of groups, gid in slot S_TMP0.
+static uint32_t group_numbers(Storage *st, Phrases &ph, DictOrder &dord, int W, uint32_t *&gid)
+{
+    const uint32_t N = (uint32_t)ph.dict_bytes;
+    PosInfo pi{ph.dphr, ph.doff, ph.dlen};
+    uint8_t *mark = slot<uint8_t>(st, S_MB, N);
+    gid = slot<uint32_t>(st, S_TMP0, N);
+    check_cuda(cudaMemsetAsync(mark, 0, N, st->stream));
+    k_mark_sheads<<<grid_for(N, 256), 256, 0, st->stream>>>(N, pi, (uint32_t)W, dord.isa, mark);
+    after_launch(st);
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, N, LoadMark{mark}, StoreGid{mark, gid}, true, (uint32_t *)st->d_scalars);
+    fetch_scalars(st, 1);
+    return (uint32_t)st->h_scalars[0];
+}
 
 // Pass 2 over dictionary positions: mark groups with differing bytes.
 __global__ void k_mark_mixed(uint32_t N, PosInfo pi, uint32_t W, const uint8_t *dict, const uint32_t *pcmin,
@@ -379,12 +394,13 @@ uint32_t run_group_index(Storage *st, Phrases &ph, DictOrder &dord, int W, uint3
 {
     const uint32_t N = (uint32_t)ph.dict_bytes;
     PosInfo pi{ph.dphr, ph.doff, ph.dlen};
+    uint32_t *gid = nullptr;
+    const uint32_t G = group_numbers(st, ph, dord, W, gid);
     grp_of = slot<uint32_t>(st, S_GRP, N);
-    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-    device_scan<uint32_t, OpAdd>(st, N, LoadSHead{dord.sa, dord.isa, pi, (uint32_t)W},
-                                 StoreGroupOnly{dord.sa, pi, (uint32_t)W, grp_of}, true, (uint32_t *)st->d_scalars);
-    fetch_scalars(st, 1);
-    return (uint32_t)st->h_scalars[0];
+    k_group_of<<<grid_for(N, 256), 256, 0, st->stream>>>(N, pi, (uint32_t)W, dord.isa, gid, grp_of, nullptr,
+                                                         nullptr, nullptr, nullptr, nullptr, nullptr);
+    after_launch(st);
+    return G;
 }
 
 void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph, DictOrder &dord,
@@ -396,15 +412,13 @@ void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph
     uint32_t *gcount = slot<uint32_t>(st, S_GCOUNT, N);
     uint16_t *gchar = slot<uint16_t>(st, S_GCHAR, N);
     uint32_t *grp_of = slot<uint32_t>(st, S_GRP, N);
-    check_cuda(cudaMemsetAsync(gcount, 0, (size_t)N * 4, st->stream));
-    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-    device_scan<uint32_t, OpAdd>(st, N, LoadSHead{dord.sa, dord.isa, pi, (uint32_t)W},
-                                 StoreSGroup{dord.sa, pi, (uint32_t)W, ph.dict, ph.occ, ph.pcmin, ph.pcmax, gcount,
-                                             gchar, grp_of},
-                                 true, (uint32_t *)st->d_scalars);
-    fetch_scalars(st, 1);
-    const uint32_t G = (uint32_t)st->h_scalars[0];
+    uint32_t *gid = nullptr;
+    const uint32_t G = group_numbers(st, ph, dord, W, gid);
     if (G == 0) throw Error{GBWT_INTERNAL_ERROR};
+    check_cuda(cudaMemsetAsync(gcount, 0, (size_t)G * 4, st->stream));
+    k_group_of<<<grid_for(N, 256), 256, 0, st->stream>>>(N, pi, (uint32_t)W, dord.isa, gid, grp_of, ph.dict, ph.occ,
+                                                         ph.pcmin, ph.pcmax, gcount, gchar);
+    after_launch(st);
     uint8_t *gmix = slot<uint8_t>(st, S_GMIX, G);
     check_cuda(cudaMemsetAsync(gmix, 0, G, st->stream));
     k_mark_mixed<<<grid_for(N, 256), 256, 0, st->stream>>>(N, pi, (uint32_t)W, ph.dict, ph.pcmin, ph.pcmax, grp_of,

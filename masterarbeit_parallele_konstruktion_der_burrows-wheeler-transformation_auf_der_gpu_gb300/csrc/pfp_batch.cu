@@ -326,11 +326,12 @@ static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dme
     after_launch(st);
     const uint2 *tseg = (const uint2 *)(dmeta + bl.o_tseg);
     // sort by (text, group) only: the byte rides along, and elements of one
-    // group keep their parse-suffix order
+    // group keep their parse-suffix order.  8-bit digits: with 4096-key tiles
+    // wider digits make the tile histograms (and their scan) as large as the
+    // keys themselves.
     const int sb = tlb + gb;
     uint32_t *nv = nullptr, *nv2 = nullptr;
-    if ((sb + 9) / 10 < (sb + 7) / 8) radix_sort<E, false, 10>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
-    else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     stage_mark(st, 5);
     k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,
                                                     (1u << bb) - 1u, dOut);
