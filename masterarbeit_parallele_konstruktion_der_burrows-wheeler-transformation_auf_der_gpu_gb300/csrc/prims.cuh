@@ -5,10 +5,12 @@
 // fly instead of being materialised.
 //
 // Radix sort: stable LSD passes over 8-bit digits.  Each pass runs a tile
-// histogram (warp-aggregated shared atomics), a digit-major exclusive scan of
-// the tile histograms, and a scatter kernel that ranks keys inside each warp
-// with __match_any_sync multisplit, reorders the tile in shared memory and
-// writes each digit's run with consecutive addresses.
+// histogram (per-warp shared atomics), a digit-major exclusive scan of the
+// tile histograms, and a scatter kernel that ranks keys inside each warp with
+// __match_any_sync multisplit, reorders the tile in shared memory and writes
+// each digit's run with consecutive addresses.  (Measured on GB300: atomics
+// beat match-aggregation for counting; for the stable ranking, match beats a
+// ballot-per-bit multisplit, whose ALU cost exceeds the match pipe's.)
 #pragma once
 #include "gbwt_internal.cuh"
 
@@ -189,6 +191,7 @@ __device__ __forceinline__ uint32_t rs_digit(K k, int shift, uint32_t mask)
     return (uint32_t)(k >> shift) & mask;
 }
 
+
 // Histogram slot of digit d for tile b.  Unsegmented: digit-major over all
 // tiles.  Segmented (tseg[b] = {first tile, tiles} of b's segment, every
 // segment a whole number of tiles): segment-major, then digit-major inside
@@ -207,20 +210,23 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__
                                                            uint32_t num_tiles, const uint2 *__restrict__ tseg)
 {
     constexpr int D = 1 << BITS;
-    __shared__ uint32_t h[D];
-    for (int d = threadIdx.x; d < D; d += RS_THREADS) h[d] = 0;
+    __shared__ uint32_t h[RS_WARPS * D];       // one histogram per warp
+    for (int d = threadIdx.x; d < RS_WARPS * D; d += RS_THREADS) h[d] = 0;
     __syncthreads();
+    uint32_t *wh = h + (threadIdx.x >> 5) * D;
     size_t base = (size_t)blockIdx.x * RS_TILE;
 #pragma unroll 4
     for (int j = 0; j < RS_ITEMS; j++) {
         size_t i = base + (size_t)j * RS_THREADS + threadIdx.x;
-        bool valid = i < n;
-        uint32_t d = valid ? rs_digit(keys[i], shift, mask) : 0xFFFFFFFFu;
-        unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        if (valid && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
+        if (i < n) atomicAdd(&wh[rs_digit(keys[i], shift, mask)], 1u);
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < D; d += RS_THREADS) tile_hist[rs_hist_index(tseg, blockIdx.x, d, num_tiles, D)] = h[d];
+    for (int d = threadIdx.x; d < D; d += RS_THREADS) {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) sum += h[w * D + d];
+        tile_hist[rs_hist_index(tseg, blockIdx.x, d, num_tiles, D)] = sum;
+    }
 }
 
 template <typename K, bool HAS_VAL, int BITS>
@@ -268,16 +274,14 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
     uint32_t *wh = s_wh + warp * D;
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; i++) {
-        uint32_t d = dg[i];
-        unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        unsigned leader = (unsigned)(__ffs(peers) - 1);
-        uint32_t prior = 0;
-        if (lane == leader && d != 0xFFFFFFFFu) {
-            prior = wh[d];
-            wh[d] = prior + (uint32_t)__popc(peers);
-        }
-        prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
+        const uint32_t d = dg[i];
+        const bool valid = d != 0xFFFFFFFFu;
+        const uint32_t dd = valid ? d : 0u;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t prior = wh[dd];
+        __syncwarp();
         rk[i] = prior + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        if (valid) wh[dd] = prior + (uint32_t)__popc(peers);    // same value from every peer
         __syncwarp();
     }
     __syncthreads();
