@@ -76,6 +76,7 @@ typedef struct gbwt_stats {
     float   stage_ms[8];    /* with GBWT_FLAG_STAGE_TIMES: scan, phrases,
                                dictionary, parse SA, S groups, runs, mixed,
                                total                                          */
+    int64_t device_bytes;   /* device scratch held by the storage now        */
 } gbwt_stats;
 
 /*
@@ -172,6 +173,63 @@ int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n
 
 /* Copies the counts of the last call into *out. */
 int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
+
+/*
+ * Frees the storage's scratch (it grows again on the next call).  No
+ * counterpart in the reference, whose device buffers are globals freed ad
+ * hoc (K:36-98); used by the serving loop to return memory to its budget.
+ */
+int64_t gbwt_trim_device_storage(void *storage);
+
+/*
+ * Serving loop.  No counterpart in the reference, which runs one text per
+ * process (main(), K:4793-4815).  A server owns `workers` host threads, each
+ * with its own storage and CUDA stream, so the work of several jobs overlaps
+ * on the device.  Jobs are admitted in arrival order while the sum of the
+ * running jobs' device-memory estimates stays within `hbm_budget` bytes
+ * (<= 0: 80 % of the free device memory at creation); a job that does not
+ * fit waits, and smaller jobs behind it may pass it.  Jobs of at most
+ * `small_max` bytes (<= 0: 16 MiB) that are waiting when a worker becomes
+ * free run together as one gbwt_pfp_bwt_batch call (continuous batching);
+ * larger jobs run alone.  Every result is what gbwt_pfp_bwt returns for the
+ * job alone.
+ *
+ * gbwt_submit queues T[0..n) -> L[0..n) (HOST buffers that must stay valid
+ * until the job is done) and returns a ticket in *ticket; gbwt_poll and
+ * gbwt_wait report the job's state in *info (may be NULL) and return
+ * GBWT_JOB_PENDING, GBWT_JOB_RUNNING, GBWT_NO_ERROR (done) or the job's
+ * error code.  gbwt_server_drain waits for every submitted job;
+ * gbwt_server_destroy drains, then joins the workers.
+ *
+ * GBWT_SERVER_SIMULATE runs the scheduler without the GPU: a job "runs" for
+ * n / 1 GB/s and copies T to L.  It exists to test the scheduling policy on
+ * machines without a GPU.
+ */
+#define GBWT_SERVER_SIMULATE 0x100u
+#define GBWT_JOB_PENDING 1
+#define GBWT_JOB_RUNNING 2
+
+typedef struct gbwt_job_info {
+    int64_t status;         /* GBWT_JOB_*, GBWT_NO_ERROR or an error code     */
+    int64_t n;              /* job length                                     */
+    int64_t est_bytes;      /* device-memory estimate it was admitted with    */
+    double  submit_us;      /* microseconds since the server was created      */
+    double  start_us;       /* its GPU call began (0 while pending)           */
+    double  end_us;         /* its result was in L (0 until done)             */
+    int32_t batch_jobs;     /* jobs in the GPU call that ran it (1 = alone)   */
+    int32_t worker;         /* worker that ran it                             */
+} gbwt_job_info;
+
+int64_t gbwt_server_create(void **server, int64_t hbm_budget, int32_t workers, int64_t small_max,
+                           uint32_t flags);
+int64_t gbwt_server_destroy(void *server);
+int64_t gbwt_submit(void *server, const uint8_t *T, uint8_t *L, int64_t n, int32_t W, int32_t P,
+                    uint32_t flags, int64_t *ticket);
+int64_t gbwt_poll(void *server, int64_t ticket, gbwt_job_info *info);
+int64_t gbwt_wait(void *server, int64_t ticket, double timeout_s, gbwt_job_info *info);
+int64_t gbwt_server_drain(void *server, double timeout_s);
+/* Largest sum of admitted estimates seen so far (bytes). */
+int64_t gbwt_server_peak_admitted(void *server);
 
 /* Kernels that can be probed (timed launch by launch with CUDA events). */
 #define GBWT_PROBE_NONE           (-1)

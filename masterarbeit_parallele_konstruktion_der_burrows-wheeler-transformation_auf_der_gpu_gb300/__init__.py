@@ -35,6 +35,9 @@ INTERNAL_ERROR = -10
 FLAG_SMALL_ALPHABET = 1
 FLAG_DEVICE_POINTERS = 2
 FLAG_STAGE_TIMES = 4
+SERVER_SIMULATE = 0x100
+JOB_PENDING = 1
+JOB_RUNNING = 2
 
 # The reference's binaries (Makefile:11-23) and their (W, P, small) variants.
 VARIANTS = {
@@ -69,7 +72,8 @@ class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int64) for k in (
         "n", "z", "d", "dict_bytes", "s", "s_elems", "mixed_blocks", "mixed_elems",
         "dict_rounds", "parse_rounds", "hash_retries", "kernel_launches", "primary_index",
-        "probe_launches", "probe_bytes")] + [("probe_ms", ctypes.c_double), ("stage_ms", ctypes.c_float * 8)]
+        "probe_launches", "probe_bytes")] + [("probe_ms", ctypes.c_double), ("stage_ms", ctypes.c_float * 8),
+                                             ("device_bytes", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}
@@ -84,8 +88,19 @@ EXPORTS = (
     "gbwt_allocate_device_storage", "gbwt_free_device_storage", "gbwt_set_stream", "gbwt_pfp_bwt",
     "gbwt_pfp_trigger_scan", "gbwt_pfp_parse", "gbwt_get_stats", "gbwt_read_input_txt",
     "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
-    "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch",
+    "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch", "gbwt_trim_device_storage",
+    "gbwt_server_create", "gbwt_server_destroy", "gbwt_submit", "gbwt_poll", "gbwt_wait", "gbwt_server_drain",
+    "gbwt_server_peak_admitted",
 )
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int64), ("n", ctypes.c_int64), ("est_bytes", ctypes.c_int64),
+                ("submit_us", ctypes.c_double), ("start_us", ctypes.c_double), ("end_us", ctypes.c_double),
+                ("batch_jobs", ctypes.c_int32), ("worker", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 PROBE_NONE = -1
 PROBE_RADIX_SCATTER = 1
@@ -133,6 +148,22 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_libcubwt_bwt.restype = i64
     L.gbwt_pfp_bwt_batch.argtypes = [vp, u8p, ctypes.c_void_p, i32, u8p, i32, i32, u32]
     L.gbwt_pfp_bwt_batch.restype = i64
+    L.gbwt_trim_device_storage.argtypes = [vp]
+    L.gbwt_trim_device_storage.restype = i64
+    L.gbwt_server_create.argtypes = [ctypes.POINTER(vp), i64, i32, i64, u32]
+    L.gbwt_server_create.restype = i64
+    L.gbwt_server_destroy.argtypes = [vp]
+    L.gbwt_server_destroy.restype = i64
+    L.gbwt_submit.argtypes = [vp, u8p, u8p, i64, i32, i32, u32, ctypes.POINTER(i64)]
+    L.gbwt_submit.restype = i64
+    L.gbwt_poll.argtypes = [vp, i64, ctypes.POINTER(JobInfo)]
+    L.gbwt_poll.restype = i64
+    L.gbwt_wait.argtypes = [vp, i64, ctypes.c_double, ctypes.POINTER(JobInfo)]
+    L.gbwt_wait.restype = i64
+    L.gbwt_server_drain.argtypes = [vp, ctypes.c_double]
+    L.gbwt_server_drain.restype = i64
+    L.gbwt_server_peak_admitted.argtypes = [vp]
+    L.gbwt_server_peak_admitted.restype = i64
     _LIB = L
     return L
 
@@ -286,6 +317,84 @@ class Storage:
                                          FLAG_SMALL_ALPHABET if small_alphabet else 0, ranks.ctypes.data,
                                          psa.ctypes.data, cap), "gbwt_pfp_parse")
         return ranks[:z].copy(), psa[:z].copy()
+
+
+class Server:
+    """Serving loop (gbwt_server_* in include/gbwt.h): jobs are admitted
+    under a device-memory budget, small ones run together as batched
+    pipeline calls, several workers overlap on the device.  ``simulate``
+    runs the same scheduler without a GPU (a job copies its text)."""
+
+    def __init__(self, hbm_budget: int = 0, workers: int = 2, small_max: int = 0, simulate: bool = False):
+        self._h = ctypes.c_void_p()
+        _check(_lib().gbwt_server_create(ctypes.byref(self._h), int(hbm_budget), int(workers), int(small_max),
+                                         SERVER_SIMULATE if simulate else 0), "gbwt_server_create")
+        self._bufs = {}
+
+    def submit(self, text, W: int = 5, P: int = 16, small_alphabet: bool = False, out=None) -> int:
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        L = np.empty(max(len(t), 1), dtype=np.uint8) if out is None else out
+        if L.dtype != np.uint8 or not L.flags.c_contiguous or len(L) < len(t):
+            raise GbwtError(BAD_PARAMETER, "submit: out must be a contiguous uint8 array of len(text) bytes")
+        ticket = ctypes.c_int64()
+        _check(_lib().gbwt_submit(self._h, t.ctypes.data, L.ctypes.data, len(t), W, P,
+                                  FLAG_SMALL_ALPHABET if small_alphabet else 0, ctypes.byref(ticket)), "gbwt_submit")
+        self._bufs[ticket.value] = (t, L)            # alive until the job is done
+        return ticket.value
+
+    def poll(self, ticket: int) -> dict:
+        if ticket not in self._bufs:
+            raise GbwtError(BAD_PARAMETER, "poll: unknown ticket")
+        info = JobInfo()
+        _lib().gbwt_poll(self._h, ticket, ctypes.byref(info))
+        return info.as_dict()
+
+    def wait(self, ticket: int, timeout: float | None = None) -> dict:
+        info = JobInfo()
+        _lib().gbwt_wait(self._h, ticket, -1.0 if timeout is None else float(timeout), ctypes.byref(info))
+        return info.as_dict()
+
+    def result(self, ticket: int) -> np.ndarray:
+        """The job's BWT (waits for it); raises GbwtError if the job failed."""
+        info = self.wait(ticket)
+        _check(info["status"], "server job")
+        t, L = self._bufs[ticket]
+        return L[:len(t)]
+
+    def release(self, ticket: int) -> None:
+        """Drops the wrapper's references to a finished job's buffers."""
+        self._bufs.pop(ticket, None)
+
+    def drain(self, timeout: float | None = None) -> None:
+        _check(_lib().gbwt_server_drain(self._h, -1.0 if timeout is None else float(timeout)), "gbwt_server_drain")
+
+    def peak_admitted(self) -> int:
+        return _lib().gbwt_server_peak_admitted(self._h)
+
+    def close(self) -> None:
+        if self._h:
+            _lib().gbwt_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def percentiles(values, qs=(50, 99)) -> dict:
+    """Nearest-rank percentiles of a list of latencies."""
+    v = np.sort(np.asarray(values, dtype=np.float64))
+    if len(v) == 0:
+        return {f"p{q}": None for q in qs}
+    return {f"p{q}": float(v[min(len(v) - 1, int(np.ceil(q / 100 * len(v))) - 1)]) for q in qs}
 
 
 _DEFAULT: Storage | None = None

@@ -410,7 +410,26 @@ extern "C" int64_t gbwt_get_stats(void *storage, gbwt_stats *out)
     Storage *st = (Storage *)storage;
     if (!st || !out) return GBWT_BAD_PARAMETER;
     *out = st->stats;
+    int64_t held = 0;
+    for (int i = 0; i < S_NUM; i++) held += (int64_t)st->slots[i].cap;
+    out->device_bytes = held;
     return GBWT_NO_ERROR;
+}
+
+extern "C" int64_t gbwt_trim_device_storage(void *storage)
+{
+    Storage *st = (Storage *)storage;
+    if (!st) return GBWT_BAD_PARAMETER;
+    return guarded([&]() -> int64_t {
+        check_cuda(cudaStreamSynchronize(st->stream));
+        for (int i = 0; i < S_NUM; i++)
+            if (st->slots[i].p) {
+                check_cuda(cudaFree(st->slots[i].p));
+                st->slots[i].p = nullptr;
+                st->slots[i].cap = 0;
+            }
+        return GBWT_NO_ERROR;
+    });
 }
 
 // ---- reference file formats (K:111-150, K:4776-4790) -----------------
