@@ -14,6 +14,15 @@ One step = one BWT (W=5, P=16) of the whole 512 MiB text.
   cpu_baseline  the CPU port of the reference's PFP (the oracle) on a
             bounded prefix of the same text, on this host's cores.
 
+Two more sections ride on the same line (rank 0):
+  batched   4096 independent texts (~512 MiB, log-normal lengths) in one
+            gbwt_pfp_bwt_batch call, device-resident and end to end, next to
+            the same texts run one call per text;
+  serving   Poisson arrivals of mixed-size jobs into the serving loop
+            (gbwt_server_*): p50/p99 latency and sustained MB/s, next to the
+            same jobs run one after another through gbwt_pfp_bwt (FIFO
+            latencies for the same arrival times).
+
 ``--impl reference`` times the reference's CPU implementation of the path:
 the reference itself is CUDA-only, so this is the oracle port (the CPU
 restatement of its PFP algorithm) on a bounded sample, rank 0 only.
@@ -287,10 +296,151 @@ def run_gpu(args):
                                              "dict_rounds", "parse_rounds", "hash_retries")},
         "stage_ms": stage["stage_ms"],
     }
+    if "batched" in args.sections:
+        line["batched"] = measure_batched(args, pkg, wl, stream)
+        log(f"[rank 0] batched: {line['batched']['value']} MB/s")
+    if "serving" in args.sections:
+        line["serving"] = measure_serving(args, pkg, wl)
+        log(f"[rank 0] serving: {line['serving']['latency_ms']}")
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+BATCH_WORKLOAD = ("4096 independent DNA texts, log-normal lengths (median 64 KiB, sigma 1.2, clipped to "
+                  "4 KiB-16 MiB, ~512 MiB total, seed 4), each 8-64 copies of its own uniform ACGT base with 0.1% "
+                  "substitutions; PFP W=5 P=16")
+
+
+def measure_batched(args, pkg, wl, stream):
+    """Config-4 batch: one gbwt_pfp_bwt_batch call per step."""
+    import numpy as np
+    import torch
+
+    concat, offsets = wl.config4_texts()
+    n = len(concat)
+    k = len(offsets) - 1
+    dev_in = torch.from_numpy(concat).cuda()
+    dev_out = torch.empty_like(dev_in)
+    host_in = torch.from_numpy(concat).pin_memory()
+    host_out = torch.empty(n, dtype=torch.uint8).pin_memory()
+    st = pkg.Storage(n)
+    st.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        st.pfp_bwt_batch_device(dev_in.data_ptr(), offsets, dev_out.data_ptr())
+    torch.cuda.synchronize()
+    steps = max(1, args.batch_steps)
+    launches = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        st.pfp_bwt_batch_device(dev_in.data_ptr(), offsets, dev_out.data_ptr())
+        launches += st.stats()["kernel_launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    st.pfp_bwt_batch_device(dev_in.data_ptr(), offsets, dev_out.data_ptr(), stage_times=True)
+    torch.cuda.synchronize()
+    stage = st.stats()
+    # end to end: pinned host texts in, host BWTs out
+    st.pfp_bwt_batch_into(host_in.numpy(), offsets, host_out.numpy())
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        st.pfp_bwt_batch_into(host_in.numpy(), offsets, host_out.numpy())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / steps
+    got = host_out.numpy()
+    if not np.array_equal(got, dev_out.cpu().numpy()):
+        raise SystemExit("bench: batched device and host paths differ")
+    # one call per text on the same device-resident texts (the same library)
+    for t in range(min(k, 32)):
+        a, b = int(offsets[t]), int(offsets[t + 1])
+        st.pfp_bwt_device(dev_in.data_ptr() + a, dev_out.data_ptr() + a, b - a)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for t in range(k):
+        a, b = int(offsets[t]), int(offsets[t + 1])
+        st.pfp_bwt_device(dev_in.data_ptr() + a, dev_out.data_ptr() + a, b - a)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    per_text_ms = e0.elapsed_time(e1)
+    if not np.array_equal(dev_out.cpu().numpy(), got):
+        raise SystemExit("bench: batched and one-call-per-text results differ")
+    st.close()
+    value = n / (ms / 1000.0) / 1e6
+    per_text_value = n / (per_text_ms / 1000.0) / 1e6
+    return {
+        "workload": BATCH_WORKLOAD, "texts": k, "n": n, "steps": steps, "value": round(value, 2), "unit": UNIT,
+        "ms_per_step": round(ms, 3), "gpu_launches_per_step": launches // steps,
+        "e2e": {"value": round(n / (e2e_ms / 1000.0) / 1e6, 2), "unit": UNIT, "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": n + 8 * (k + 1), "d2h_bytes_per_step": n},
+        "one_call_per_text": {"value": round(per_text_value, 2), "unit": UNIT, "ms": round(per_text_ms, 1),
+                              "calls": k},
+        "speedup_vs_one_call_per_text": round(value / per_text_value, 2),
+        "stage_ms": stage["stage_ms"],
+    }
+
+
+def measure_serving(args, pkg, wl):
+    """Config-5 serving: Poisson arrivals into the serving loop."""
+    import numpy as np
+
+    texts, arrivals = wl.serving_jobs(args.serve_jobs, args.serve_rate)
+    total = int(sum(len(t) for t in texts))
+    small_max = 16 << 20
+    with pkg.Server(workers=2, small_max=small_max) as srv:
+        # warm-up: one large job and a burst of small ones
+        warm = [srv.submit(t) for t in texts[:64]]
+        warm.append(srv.submit(max(texts, key=len)))
+        srv.drain()
+        outs = [np.empty(len(t), np.uint8) for t in texts]
+        t0 = time.perf_counter()
+        tickets = []
+        for t, at, o in zip(texts, arrivals, outs):
+            delay = at - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append(srv.submit(t, out=o))
+        srv.drain()
+        infos = [srv.poll(k) for k in tickets]
+    if any(i["status"] != 0 for i in infos):
+        raise SystemExit("bench: a serving job failed")
+    lat = [(i["end_us"] - i["submit_us"]) / 1000.0 for i in infos]
+    span_s = (max(i["end_us"] for i in infos) - min(i["submit_us"] for i in infos)) / 1e6
+    # the same jobs, one gbwt_pfp_bwt call after another (FIFO for the same arrivals)
+    st = pkg.Storage(max(len(t) for t in texts))
+    for t in texts[:16]:
+        st.pfp_bwt(t)
+    service = []
+    for t, o in zip(texts, outs):
+        a = time.perf_counter()
+        L = st.pfp_bwt(t)
+        service.append(time.perf_counter() - a)
+        if not np.array_equal(L, o):
+            raise SystemExit("bench: serving result differs from the job run alone")
+    st.close()
+    fifo, end = [], 0.0
+    for at, sv in zip(arrivals, service):
+        start = max(at, end)
+        end = start + sv
+        fifo.append((end - at) * 1000.0)
+    small = [l for l, t in zip(lat, texts) if len(t) <= small_max]
+    large = [l for l, t in zip(lat, texts) if len(t) > small_max]
+    return {
+        "workload": (f"{len(texts)} jobs, Poisson arrivals at {args.serve_rate:g}/s; ~1% 64-256 MiB repetitive DNA "
+                     "(prefixes of one text built like the 512 MiB workload), the rest with the batched workload's "
+                     "log-normal lengths; W=5 P=16; 2 workers, jobs <= 16 MiB batched"),
+        "jobs": len(texts), "bytes": total, "large_jobs": len(large),
+        "latency_ms": pkg.percentiles(lat), "latency_ms_small": pkg.percentiles(small),
+        "latency_ms_large": pkg.percentiles(large),
+        "sustained": {"value": round(total / span_s / 1e6, 2), "unit": UNIT},
+        "max_batch_jobs": max(i["batch_jobs"] for i in infos),
+        "sequential": {"value": round(total / sum(service) / 1e6, 2), "unit": UNIT,
+                       "latency_ms": pkg.percentiles(fifo)},
+    }
 
 
 def traffic_per_launch(per_launch_bytes):
@@ -312,6 +462,11 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbwt", choices=["gbwt", "reference"])
     ap.add_argument("--cpu-sample-mib", type=int, default=16)
+    ap.add_argument("--sections", default="plain,batched,serving",
+                    help="comma list: the plain headline always runs; batched, serving are extra sections")
+    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--serve-jobs", type=int, default=800)
+    ap.add_argument("--serve-rate", type=float, default=1000.0)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("bench: warm-up raised to 3 steps")

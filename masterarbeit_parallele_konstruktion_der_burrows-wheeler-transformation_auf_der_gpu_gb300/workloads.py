@@ -153,3 +153,38 @@ def batch_texts(count: int = 4096, scale: float = 1.0, seed: int = 4, sub_rate: 
 def config4_texts(scale: float = 1.0):
     """4096 texts, about 512 MiB in total (seed 4)."""
     return batch_texts(4096, scale, seed=4)
+
+
+def serving_jobs(count: int = 800, rate: float = 1000.0, seed: int = 5, large_frac: float = 0.01,
+                 large_lo: int = 64 * MiB, large_hi: int = 256 * MiB):
+    """Serving workload: `count` jobs with Poisson arrivals (`rate` per
+    second).  A fraction `large_frac` are large repetitive-DNA texts of
+    large_lo..large_hi bytes, cut from one text built like the 512 MiB
+    workload (4 MiB base, mutated copies with substitutions and indels);
+    the others have the batched workload's log-normal lengths, each text
+    8..64 mutated copies of its own base.  Returns (texts, arrival times in
+    seconds from the first arrival)."""
+    rng = np.random.default_rng(seed)
+    is_large = rng.random(count) < large_frac
+    if count and not is_large.any():
+        is_large[count // 2] = True
+    lens = batch_lengths(count, seed=seed + 1)
+    big = None
+    if is_large.any():
+        big_len = int(large_hi)
+        copies = max(1, big_len // (4 * MiB) + 1)
+        big = dna_copies(4 * MiB, copies, 1e-3, seed=seed + 2, indel_rate=1e-4)[:big_len]
+    texts = []
+    for i in range(count):
+        if is_large[i]:
+            ln = int(rng.integers(large_lo, large_hi + 1))
+            texts.append(big[:ln])
+        else:
+            ln = int(lens[i])
+            copies = int(rng.integers(8, 65))
+            base = DNA[rng.integers(0, 4, size=max(1, ln // copies))]
+            t = np.tile(base, copies + 1)[:ln]
+            texts.append(_substitute(rng, t, 1e-3))
+    gaps = rng.exponential(1.0 / rate, size=count)
+    gaps[0] = 0.0
+    return texts, np.cumsum(gaps)
