@@ -248,6 +248,22 @@ def run_gpu(args):
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
 
+    # ---- inverse BWT on the GPU (round trip of the timed output) -----------
+    primary = stage["primary_index"]
+    dev_back = torch.empty_like(dev_text)
+    st.unbwt_device(dev_out.data_ptr(), dev_back.data_ptr(), n, primary)
+    torch.cuda.synchronize()
+    u0, u1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    u0.record(stream)
+    for _ in range(3):
+        st.unbwt_device(dev_out.data_ptr(), dev_back.data_ptr(), n, primary)
+    u1.record(stream)
+    torch.cuda.synchronize()
+    unbwt_ms = u0.elapsed_time(u1) / 3
+    if not torch.equal(dev_back, dev_text):
+        raise SystemExit("bench: inverse BWT does not give the text back")
+    del dev_back
+
     # ---- correctness of what was timed (size-independent checks) ----------
     got = host_out.numpy()
     if not np.array_equal(np.bincount(got, minlength=256), np.bincount(text, minlength=256)):
@@ -292,6 +308,8 @@ def run_gpu(args):
                                    f"({cpu_dt:.1f} s)"},
         "clocks": clocks,
         "gpu_launches": launches,
+        "inverse_bwt": {"value": round(n / (unbwt_ms / 1000.0) / 1e6, 2), "unit": UNIT, "ms": round(unbwt_ms, 3),
+                        "check": "gbwt_unbwt(BWT, primary index) == text"},
         "pipeline": {k: stats[k] for k in ("z", "d", "dict_bytes", "s", "mixed_blocks", "mixed_elems",
                                              "dict_rounds", "parse_rounds", "hash_retries")},
         "stage_ms": stage["stage_ms"],

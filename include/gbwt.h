@@ -171,6 +171,24 @@ int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, in
  */
 int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n);
 
+/*
+ * Inverse BWT on the GPU: L[0..n) as returned by gbwt_pfp_bwt and its
+ * primary index (gbwt_stats.primary_index) -> T[0..n).  Host pointers, or
+ * device pointers with GBWT_FLAG_DEVICE_POINTERS.  Returns n;
+ * GBWT_BAD_PARAMETER when L is not a BWT with that primary index.  The
+ * reference declares libcubwt_unbwt without defining it (libcubwt.cuh:101).
+ */
+int64_t gbwt_unbwt(void *storage, const uint8_t *L, uint8_t *T, int64_t n, int64_t primary, uint32_t flags);
+
+/*
+ * libcubwt_unbwt's contract (libcubwt.cuh:90-101): T is libcubwt's BWT
+ * (L[0] = T[n-1], no '$' row), i its primary index, U the output (host
+ * pointers; may equal T); freq may be NULL (counts are recomputed).
+ * Returns GBWT_NO_ERROR.
+ */
+int64_t gbwt_libcubwt_unbwt(void *storage, const uint8_t *T, uint8_t *U, int64_t n, const int32_t *freq,
+                            int32_t i);
+
 /* Copies the counts of the last call into *out. */
 int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
 

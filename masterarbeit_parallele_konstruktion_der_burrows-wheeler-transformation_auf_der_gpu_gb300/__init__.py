@@ -90,7 +90,7 @@ EXPORTS = (
     "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
     "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch", "gbwt_trim_device_storage",
     "gbwt_server_create", "gbwt_server_destroy", "gbwt_submit", "gbwt_poll", "gbwt_wait", "gbwt_server_drain",
-    "gbwt_server_peak_admitted",
+    "gbwt_server_peak_admitted", "gbwt_unbwt", "gbwt_libcubwt_unbwt",
 )
 
 
@@ -148,6 +148,10 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_libcubwt_bwt.restype = i64
     L.gbwt_pfp_bwt_batch.argtypes = [vp, u8p, ctypes.c_void_p, i32, u8p, i32, i32, u32]
     L.gbwt_pfp_bwt_batch.restype = i64
+    L.gbwt_unbwt.argtypes = [vp, u8p, u8p, i64, i64, u32]
+    L.gbwt_unbwt.restype = i64
+    L.gbwt_libcubwt_unbwt.argtypes = [vp, u8p, u8p, i64, ctypes.c_void_p, i32]
+    L.gbwt_libcubwt_unbwt.restype = i64
     L.gbwt_trim_device_storage.argtypes = [vp]
     L.gbwt_trim_device_storage.restype = i64
     L.gbwt_server_create.argtypes = [ctypes.POINTER(vp), i64, i32, i64, u32]
@@ -282,6 +286,25 @@ class Storage:
         idx = _check(_lib().gbwt_libcubwt_bwt(self.handle, t.ctypes.data, out.ctypes.data, len(t)),
                      "gbwt_libcubwt_bwt")
         return out[:len(t)], idx
+
+    def unbwt(self, L, primary: int) -> np.ndarray:
+        """Inverse BWT on the GPU of gbwt_pfp_bwt's output and its primary index."""
+        b = _host_u8(L)
+        T = np.empty(max(len(b), 1), dtype=np.uint8)
+        _check(_lib().gbwt_unbwt(self.handle, b.ctypes.data, T.ctypes.data, len(b), int(primary), 0), "gbwt_unbwt")
+        return T[:len(b)]
+
+    def unbwt_device(self, L_ptr: int, T_ptr: int, n: int, primary: int) -> int:
+        return _check(_lib().gbwt_unbwt(self.handle, ctypes.c_void_p(L_ptr), ctypes.c_void_p(T_ptr), n, int(primary),
+                                        FLAG_DEVICE_POINTERS), "gbwt_unbwt")
+
+    def libcubwt_unbwt(self, L, primary: int) -> np.ndarray:
+        """libcubwt_unbwt semantics: libcubwt's BWT and primary index -> text."""
+        b = _host_u8(L)
+        U = np.empty(max(len(b), 1), dtype=np.uint8)
+        _check(_lib().gbwt_libcubwt_unbwt(self.handle, b.ctypes.data, U.ctypes.data, len(b), None, int(primary)),
+               "gbwt_libcubwt_unbwt")
+        return U[:len(b)]
 
     def set_kernel_probe(self, kernel: int) -> None:
         """Time every launch of one kernel family (PROBE_*) from now on."""

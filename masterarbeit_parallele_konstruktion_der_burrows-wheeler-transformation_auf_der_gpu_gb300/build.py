@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libgbwt.so")
 CLI = os.path.join(HERE, "gbwt_pfp")
 
 CU_SOURCES = ["pfp_scan.cu", "pfp_phrases.cu", "pfp_sort.cu", "pfp_assembly.cu", "pfp_batch.cu", "gbwt_api.cu",
-              "gbwt_serve.cu"]
+              "gbwt_serve.cu", "pfp_unbwt.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -247,6 +247,67 @@ extern "C" int64_t gbwt_pfp_bwt(void *storage, const uint8_t *T, uint8_t *L, int
     return guarded([&]() { return pipeline(st, T, L, n, W, P, flags, UPTO_BWT, nullptr); });
 }
 
+// Inverse BWT: the PFP output convention (primary = gbwt_stats.primary_index)
+// or libcubwt's (its primary index, L without the '$' row).
+static int64_t unbwt_common(Storage *st, const uint8_t *L, uint8_t *T, int64_t n, int64_t primary, bool pfp,
+                            bool devptr)
+{
+    if (n < 0 || n > MAX_N) return GBWT_BAD_PARAMETER;
+    if (n == 0) return 0;
+    if (!L || !T) return GBWT_BAD_PARAMETER;
+    if (pfp ? (primary < 0 || primary >= n) : (primary < 1 || primary > n)) return GBWT_BAD_PARAMETER;
+    memset(&st->stats, 0, sizeof(st->stats));
+    st->launches = 0;
+    st->stats.n = n;
+    const uint32_t un = (uint32_t)n;
+    const uint8_t *dL;
+    uint8_t *dT;
+    if (devptr) {
+        dL = L;
+        dT = T;
+    } else {
+        uint8_t *buf = slot<uint8_t>(st, S_TEXT, (size_t)n + 16);
+        check_cuda(cudaMemcpyAsync(buf, L, (size_t)n, cudaMemcpyHostToDevice, st->stream));
+        dL = buf;
+        dT = slot<uint8_t>(st, S_OUT, (size_t)n + 16);
+    }
+    check_cuda(cudaMemsetAsync(st->d_flags, 0, 64 * sizeof(uint32_t), st->stream));
+    const uint8_t *dLc = dL;
+    if (pfp) {
+        uint8_t *lc = slot<uint8_t>(st, S_LCB, (size_t)n + 16);
+        pfp_to_libcubwt(st, dL, un, (uint32_t)primary, lc);
+        dLc = lc;
+    }
+    run_unbwt(st, dLc, un, pfp ? (uint32_t)primary + 1u : (uint32_t)primary, dT);
+    if (!devptr) check_cuda(cudaMemcpyAsync(T, dT, (size_t)n, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 8, st->d_flags, 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    if ((uint32_t)st->h_scalars[8] & ERR_INTERNAL) return GBWT_INTERNAL_ERROR;
+    st->stats.kernel_launches = st->launches;
+    return n;
+}
+
+extern "C" int64_t gbwt_unbwt(void *storage, const uint8_t *L, uint8_t *T, int64_t n, int64_t primary, uint32_t flags)
+{
+    Storage *st = (Storage *)storage;
+    if (!st) return GBWT_BAD_PARAMETER;
+    return guarded([&]() {
+        return unbwt_common(st, L, T, n, primary, true, (flags & GBWT_FLAG_DEVICE_POINTERS) != 0);
+    });
+}
+
+extern "C" int64_t gbwt_libcubwt_unbwt(void *storage, const uint8_t *T, uint8_t *U, int64_t n, const int32_t *freq,
+                                       int32_t i)
+{
+    (void)freq;       // recomputed on the device
+    Storage *st = (Storage *)storage;
+    if (!st) return GBWT_BAD_PARAMETER;
+    return guarded([&]() -> int64_t {
+        const int64_t rc = unbwt_common(st, T, U, n, i, false, false);
+        return rc < 0 ? rc : GBWT_NO_ERROR;
+    });
+}
+
 extern "C" int64_t gbwt_pfp_bwt_batch(void *storage, const uint8_t *T_concat, const int64_t *offsets, int32_t k,
                                       uint8_t *L_concat, int32_t W, int32_t P, uint32_t flags)
 {

@@ -218,6 +218,9 @@ void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph
 
 void stage_mark(Storage *st, int idx);
 
+void pfp_to_libcubwt(Storage *st, const uint8_t *dO, uint32_t n, uint32_t p, uint8_t *dLc);
+void run_unbwt(Storage *st, const uint8_t *dLc, uint32_t n, uint32_t i, uint8_t *dT);
+
 int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t k, uint8_t *L, int W, int P,
                   uint32_t flags, int64_t max_n);
 

@@ -232,19 +232,28 @@ __global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, 
     }
 }
 
-// Host layout of a batch: the non-empty texts in X, and the segments.
+// Host layout of a batch: the non-empty texts in X, and the segments.  One
+// text per segment when its tile padding costs at most 1/8 of the elements
+// (the key then needs no text bits); otherwise texts are grouped until a
+// segment holds SEG_MIN elements.
 static BatchLayout batch_layout(Storage *st, const int64_t *offsets, int32_t k, int W)
 {
     BatchLayout bl;
     bl.total = (uint64_t)offsets[k];
     uint32_t kk = 0;
-    uint64_t tiles = 0, seg_real = 0;
+    uint64_t tiles = 0, seg_real = 0, single_tiles = 0;
+    for (int32_t t = 0; t < k; t++) {
+        const uint64_t len = (uint64_t)(offsets[t + 1] - offsets[t]);
+        if (!len) continue;
+        single_tiles += (len + RS_TILE - 1) / RS_TILE;
+    }
+    const uint64_t seg_min = single_tiles * RS_TILE <= bl.total + bl.total / 8 ? 1u : SEG_MIN;
     for (int32_t t = 0; t < k; t++) {
         const uint64_t len = (uint64_t)(offsets[t + 1] - offsets[t]);
         if (!len) continue;
         kk++;
         seg_real += len;
-        if (seg_real >= SEG_MIN) {
+        if (seg_real >= seg_min) {
             tiles += (seg_real + RS_TILE - 1) / RS_TILE;
             seg_real = 0;
         }
@@ -301,7 +310,7 @@ static BatchLayout batch_layout(Storage *st, const int64_t *offsets, int32_t k, 
         x += len + (uint64_t)W;
         seg_real += len;
         i++;
-        if (seg_real >= SEG_MIN) close_segment(i);
+        if (seg_real >= seg_min) close_segment(i);
     }
     if (seg_real) close_segment(i);
     xs[kk] = (uint32_t)x;
@@ -326,12 +335,13 @@ static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dme
     after_launch(st);
     const uint2 *tseg = (const uint2 *)(dmeta + bl.o_tseg);
     // sort by (text, group) only: the byte rides along, and elements of one
-    // group keep their parse-suffix order.  8-bit digits: with 4096-key tiles
-    // wider digits make the tile histograms (and their scan) as large as the
-    // keys themselves.
+    // group keep their parse-suffix order.  9-bit digits when they save a
+    // pass (e.g. 25 group bits: 3 passes instead of 4); wider digits make the
+    // 4096-key tiles' histograms (and their scan) too large.
     const int sb = tlb + gb;
     uint32_t *nv = nullptr, *nv2 = nullptr;
-    radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    if ((sb + 8) / 9 < (sb + 7) / 8) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     stage_mark(st, 5);
     k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,
                                                     (1u << bb) - 1u, dOut);

@@ -214,11 +214,27 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *__restrict__
     for (int d = threadIdx.x; d < RS_WARPS * D; d += RS_THREADS) h[d] = 0;
     __syncthreads();
     uint32_t *wh = h + (threadIdx.x >> 5) * D;
-    size_t base = (size_t)blockIdx.x * RS_TILE;
+    const size_t base = (size_t)blockIdx.x * RS_TILE;
+    constexpr int KPV = 16 / (int)sizeof(K);          // keys per 16-byte load
+    constexpr int NV = RS_ITEMS / KPV;
+    if (base + RS_TILE <= n && (((uintptr_t)keys) & 15u) == 0) {
+        // full tile: every load issued before any count (counting needs no order)
+        uint4 v[NV];
+#pragma unroll
+        for (int j = 0; j < NV; j++) v[j] = __ldg((const uint4 *)(keys + base) + (size_t)j * RS_THREADS + threadIdx.x);
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            K kk[KPV];
+            memcpy(kk, &v[j], 16);
+#pragma unroll
+            for (int q = 0; q < KPV; q++) atomicAdd(&wh[rs_digit(kk[q], shift, mask)], 1u);
+        }
+    } else {
 #pragma unroll 4
-    for (int j = 0; j < RS_ITEMS; j++) {
-        size_t i = base + (size_t)j * RS_THREADS + threadIdx.x;
-        if (i < n) atomicAdd(&wh[rs_digit(keys[i], shift, mask)], 1u);
+        for (int j = 0; j < RS_ITEMS; j++) {
+            size_t i = base + (size_t)j * RS_THREADS + threadIdx.x;
+            if (i < n) atomicAdd(&wh[rs_digit(keys[i], shift, mask)], 1u);
+        }
     }
     __syncthreads();
     for (int d = threadIdx.x; d < D; d += RS_THREADS) {

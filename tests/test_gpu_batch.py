@@ -111,3 +111,13 @@ def test_batch_scaled_mix_round_trip(storage, orc, wl):
         t = concat[offsets[i]:offsets[i + 1]]
         L = out[offsets[i]:offsets[i + 1]]
         assert np.array_equal(L, orc.sa_bwt(t)), i
+
+
+def test_batch_one_text_per_segment(storage, orc, wl):
+    # lengths that are whole radix tiles: no padding, so every text gets its own sort segment
+    rng = np.random.default_rng(14)
+    texts = [wl.dna_copies(base_len=512 * int(rng.integers(1, 5)), copies=8, seed=200 + i)[:4096 * int(rng.integers(1, 4))]
+             for i in range(12)]
+    got = storage.pfp_bwt_batch(texts)
+    for i, t in enumerate(texts):
+        assert np.array_equal(got[i], orc.sa_bwt(t)), i

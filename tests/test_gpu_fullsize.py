@@ -29,6 +29,8 @@ def test_512mib_dna_variants_agree_and_invert(pkg, orc, dna512):
     assert np.array_equal(a, c)
     assert np.array_equal(np.bincount(a, minlength=256), np.bincount(t, minlength=256))
     assert np.array_equal(orc.unbwt(a, pidx), t)
+    with pkg.Storage(len(t)) as st:
+        assert np.array_equal(st.unbwt(a, pidx), t)          # the GPU inverse, same round trip
 
 
 def test_versioned_markov_inverts(pkg, orc, wl):
