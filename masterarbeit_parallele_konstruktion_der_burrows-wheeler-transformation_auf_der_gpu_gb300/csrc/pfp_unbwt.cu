@@ -11,20 +11,22 @@
 //          multisplit, as in the radix downsweep) that writes LF in row
 //          order, so nothing is scattered.
 //   walk   T[n-1-k] = B[LF^k(0)].  Rows whose hash falls in 1/rate are
-//          rulers (row 0 always); one thread per ruler follows LF to the
-//          next ruler (bit 31 of an LF entry marks a ruler target) and
-//          records the distance; the host ranks the short ruler chain; a
+//          rulers (row 0 always); an LF entry whose target is a ruler holds
+//          bit 31 | the ruler's index.  One thread per ruler follows LF to
+//          the next ruler and records the distance; pointer jumping over
+//          the ruler chain gives every ruler its distance from row 0; a
 //          second walk writes every text byte.  The symbol of a row comes
 //          from the bucket its LF value falls in, so a step reads one word.
 // Walks end at the next ruler; the rulers split the single LF cycle, so the
 // steps of all walks sum to n+1.  A BWT whose LF has more than one cycle is
-// rejected (the chain of rulers does not cover them all).
+// rejected (the ruler chain from row 0 is not one list through all rulers,
+// or does not come back to row 0 after n+1 steps).
 #include "prims.cuh"
-#include <vector>
 
 namespace gbwt {
 
 constexpr uint32_t UB_RULER = 0x80000000u;
+constexpr uint32_t UB_NIL = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint32_t ub_mix(uint32_t x)
 {
@@ -48,11 +50,24 @@ __global__ void k_pfp_to_libcubwt(const uint8_t *O, uint32_t n, uint32_t p, uint
     Lc[e] = e == 0 ? O[p] : (e <= p ? O[e - 1] : O[e]);
 }
 
-// LF of every row.  Element e of Lc is row e (e < i) or e+1 (e >= i).
+// Index of ruler row t in the sorted ruler list.
+__device__ __forceinline__ uint32_t ub_ruler_index(const uint32_t *rul, uint32_t m, uint32_t t)
+{
+    uint32_t lo = 0, hi = m - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rul[mid] < t) lo = mid + 1u; else hi = mid;
+    }
+    return lo;
+}
+
+// LF of every row.  Element e of Lc is row e (e < i) or e+1 (e >= i).  An
+// entry whose target row is a ruler holds UB_RULER | the ruler's index.
 template <int BITS>
 __global__ void __launch_bounds__(RS_THREADS) k_lf_rank(const uint8_t *__restrict__ Lc, uint32_t n, uint32_t i,
                                                         const uint32_t *__restrict__ tile_off, uint32_t num_tiles,
-                                                        uint32_t rate_mask, uint32_t *__restrict__ LF)
+                                                        uint32_t rate_mask, const uint32_t *__restrict__ rul,
+                                                        uint32_t m, uint32_t *__restrict__ LF)
 {
     constexpr int D = 1 << BITS;
     constexpr int DPT = D / RS_THREADS;
@@ -105,9 +120,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_lf_rank(const uint8_t *__restric
         // position among all non-'$' rows of this symbol's bucket
         const uint32_t t = 1u + s_goff[d] + s_wh[warp * D + d] + rk[q];
         const uint32_t row = (uint32_t)e < i ? (uint32_t)e : (uint32_t)e + 1u;
-        LF[row] = t | (ub_is_ruler(t, rate_mask) ? UB_RULER : 0u);
+        LF[row] = ub_is_ruler(t, rate_mask) ? (UB_RULER | ub_ruler_index(rul, m, t)) : t;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) LF[i] = 0u | UB_RULER;     // '$' row -> row 0
+    if (blockIdx.x == 0 && threadIdx.x == 0) LF[i] = UB_RULER | 0u;      // '$' row -> row 0 = ruler 0
 }
 
 struct LoadRuler {
@@ -125,33 +140,59 @@ struct StoreRuler {
     }
 };
 
-// Pass 1: distance from each ruler to the next one along LF.
-__global__ void k_walk_count(const uint32_t *LF, const uint32_t *rul, uint32_t m, uint32_t rows, uint32_t *nxt,
-                             uint32_t *dist, uint32_t *flags)
+// Pass 1: next ruler and distance from each ruler along LF.  The ruler
+// whose successor is ruler 0 ends the chain (no successor; its weight is
+// the last hop back to row 0).
+__global__ void k_walk_count(const uint32_t *LF, const uint32_t *rul, uint32_t m, uint32_t rows, uint32_t *succ,
+                             uint64_t *wt, uint32_t *flags)
 {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
     uint32_t r = rul[j], steps = 0, v;
-    do {
+    for (;;) {
         v = __ldg(LF + r);
-        r = v & ~UB_RULER;
         steps++;
-    } while (!(v & UB_RULER) && steps <= rows);
-    if (steps > rows) atomicOr(flags, ERR_INTERNAL);
-    uint32_t lo = 0, hi = m - 1u;            // ruler index of row r
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (rul[mid] < r) lo = mid + 1u; else hi = mid;
+        if ((v & UB_RULER) || steps > rows) break;
+        r = v;
     }
-    if (rul[lo] != r) atomicOr(flags, ERR_INTERNAL);
-    nxt[j] = lo;
-    dist[j] = steps;
+    if (steps > rows) atomicOr(flags, ERR_INTERNAL);
+    const uint32_t nx = v & ~UB_RULER;
+    succ[j] = nx == 0 ? UB_NIL : nx;
+    wt[j] = steps;
+}
+
+// Pointer jumping (list ranking): after r rounds wt[j] is the distance over
+// the next 2^r rulers (or to the chain's end).  Double-buffered; `open`
+// counts rulers that still have a successor.
+__global__ void k_jump(const uint32_t *succ, const uint64_t *wt, uint32_t m, uint32_t *succ2, uint64_t *wt2,
+                       uint32_t *open)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const uint32_t s = succ[j];
+    if (s == UB_NIL) {
+        succ2[j] = UB_NIL;
+        wt2[j] = wt[j];
+        return;
+    }
+    wt2[j] = wt[j] + wt[s];
+    const uint32_t s2 = succ[s];
+    succ2[j] = s2;
+    if (s2 != UB_NIL) atomicAdd(open, 1u);
+}
+
+// Offsets from row 0: off[j] = total - (distance from ruler j to the end).
+__global__ void k_ruler_off(const uint64_t *wt, uint32_t m, uint32_t *off)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    off[j] = (uint32_t)(wt[0] - wt[j]);
 }
 
 // Pass 2: every ruler writes the text bytes of its stretch.  sym(row) is
 // the bucket of LF(row)-1 among the cumulative symbol counts cum[0..256].
-__global__ void k_walk_emit(const uint32_t *LF, const uint32_t *rul, const uint32_t *off, const uint32_t *dist,
-                            uint32_t m, const uint32_t *cum, uint32_t n, uint8_t *T)
+__global__ void k_walk_emit(const uint32_t *LF, const uint32_t *rul, const uint32_t *off, uint32_t m,
+                            const uint32_t *cum, uint32_t n, uint8_t *T)
 {
     __shared__ uint32_t s_cum[257];
     for (int c = threadIdx.x; c < 257; c += blockDim.x) s_cum[c] = cum[c];
@@ -159,10 +200,10 @@ __global__ void k_walk_emit(const uint32_t *LF, const uint32_t *rul, const uint3
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
     uint32_t r = rul[j], k = off[j];
-    const uint32_t steps = dist[j];
-    for (uint32_t s = 0; s < steps; s++, k++) {
+    for (uint32_t s = 0; s <= n; s++, k++) {
         const uint32_t v = __ldg(LF + r);
-        const uint32_t t = v & ~UB_RULER;
+        const bool last = (v & UB_RULER) != 0;
+        const uint32_t t = last ? rul[v & ~UB_RULER] : v;
         if (k < n && t > 0) {
             uint32_t lo = 0, hi = 255;           // last c with cum[c] <= t-1
             while (lo < hi) {
@@ -171,6 +212,7 @@ __global__ void k_walk_emit(const uint32_t *LF, const uint32_t *rul, const uint3
             }
             T[n - 1u - k] = (uint8_t)lo;
         }
+        if (last) break;
         r = t;
     }
 }
@@ -193,58 +235,57 @@ void pfp_to_libcubwt(Storage *st, const uint8_t *dO, uint32_t n, uint32_t p, uin
 void run_unbwt(Storage *st, const uint8_t *dLc, uint32_t n, uint32_t i, uint8_t *dT)
 {
     const uint32_t rows = n + 1u;
+    // ~1/128 of the rows are rulers: the longest walk (about 128 ln m steps of
+    // one dependent load each) sets the time of both walk passes
     uint32_t rate = 16;
-    while (rate < (1u << 20) && (uint64_t)rate * 262144u < rows) rate <<= 1;
+    while (rate < 128 && (uint64_t)rate * 65536u < rows) rate <<= 1;
     const uint32_t rate_mask = rate - 1u;
-    const uint32_t num_tiles = (uint32_t)(((size_t)n + RS_TILE - 1) / RS_TILE);
-    uint32_t *hist = slot<uint32_t>(st, S_RSHIST, (size_t)256 * num_tiles);
-    k_rs_upsweep<uint8_t, 8><<<num_tiles, RS_THREADS, 0, st->stream>>>(dLc, n, 0, 0xFFu, hist, num_tiles, nullptr);
-    after_launch(st);
-    scan_array_excl<uint32_t, OpAdd>(st, hist, (size_t)256 * num_tiles, 0);
-    uint32_t *LF = slot<uint32_t>(st, S_ISA, rows);
-    k_lf_rank<8><<<num_tiles, RS_THREADS, 0, st->stream>>>(dLc, n, i, hist, num_tiles, rate_mask, LF);
-    after_launch(st);
-    uint32_t *cum = slot<uint32_t>(st, S_TMP2, 257);
-    k_unbwt_cum<<<1, 256, 0, st->stream>>>(hist, num_tiles, n, cum);
-    after_launch(st);
     // rulers in row order
     check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
     uint32_t *rul = slot<uint32_t>(st, S_SA, rows / 2 + 1024);
     device_scan<uint32_t, OpAdd>(st, rows, LoadRuler{rate_mask}, StoreRuler{rul}, false, (uint32_t *)st->d_scalars);
     fetch_scalars(st, 1);
     const uint32_t m = (uint32_t)st->h_scalars[0];
-    if (m == 0 || m > rows / 2 + 1024) throw Error{GBWT_INTERNAL_ERROR};
-    uint32_t *nxt = slot<uint32_t>(st, S_TMP0, m);
-    uint32_t *dist = slot<uint32_t>(st, S_TMP1, m);
-    uint32_t *off = slot<uint32_t>(st, S_VAL0, m);
-    k_walk_count<<<grid_for(m, 128), 128, 0, st->stream>>>(LF, rul, m, rows, nxt, dist, st->d_flags);
+    if (m == 0 || m > rows / 2 + 1024 || m >= UB_RULER) throw Error{GBWT_INTERNAL_ERROR};
+    // LF
+    const uint32_t num_tiles = (uint32_t)(((size_t)n + RS_TILE - 1) / RS_TILE);
+    uint32_t *hist = slot<uint32_t>(st, S_RSHIST, (size_t)256 * num_tiles);
+    k_rs_upsweep<uint8_t, 8><<<num_tiles, RS_THREADS, 0, st->stream>>>(dLc, n, 0, 0xFFu, hist, num_tiles, nullptr);
     after_launch(st);
-    // rank the ruler chain on the host (m is about rows / rate)
-    if (st->h_meta_cap < (size_t)3 * m) {
-        if (st->h_meta) check_cuda(cudaFreeHost(st->h_meta));
-        st->h_meta = nullptr;
-        st->h_meta_cap = 0;
-        const size_t cap = (size_t)3 * m + 1024;
-        check_cuda(cudaHostAlloc(&st->h_meta, cap * sizeof(uint32_t), cudaHostAllocDefault));
-        st->h_meta_cap = cap;
+    scan_array_excl<uint32_t, OpAdd>(st, hist, (size_t)256 * num_tiles, 0);
+    uint32_t *LF = slot<uint32_t>(st, S_ISA, rows);
+    k_lf_rank<8><<<num_tiles, RS_THREADS, 0, st->stream>>>(dLc, n, i, hist, num_tiles, rate_mask, rul, m, LF);
+    after_launch(st);
+    uint32_t *cum = slot<uint32_t>(st, S_TMP2, 257);
+    k_unbwt_cum<<<1, 256, 0, st->stream>>>(hist, num_tiles, n, cum);
+    after_launch(st);
+    // walk 1 and list ranking of the ruler chain
+    uint32_t *succ = slot<uint32_t>(st, S_TMP0, m), *succ2 = slot<uint32_t>(st, S_TMP1, m);
+    uint64_t *wt = slot<uint64_t>(st, S_KEY0, m), *wt2 = slot<uint64_t>(st, S_KEY1, m);
+    k_walk_count<<<grid_for(m, 128), 128, 0, st->stream>>>(LF, rul, m, rows, succ, wt, st->d_flags);
+    after_launch(st);
+    // one list of m rulers closes after ceil(log2 m) rounds; anything still
+    // open then lies on a cycle that does not pass row 0
+    const int rounds = bits_for(m) + 1;
+    for (int r = 0; r < rounds; r++) {
+        if (r == rounds - 1) check_cuda(cudaMemsetAsync(st->d_flags + 4, 0, 4, st->stream));
+        k_jump<<<grid_for(m, 256), 256, 0, st->stream>>>(succ, wt, m, succ2, wt2, st->d_flags + 4);
+        after_launch(st);
+        uint32_t *ts = succ; succ = succ2; succ2 = ts;
+        uint64_t *tw = wt; wt = wt2; wt2 = tw;
     }
-    uint32_t *hn = st->h_meta, *hd = st->h_meta + m, *ho = st->h_meta + 2 * (size_t)m;
-    check_cuda(cudaMemcpyAsync(hn, nxt, (size_t)m * 4, cudaMemcpyDeviceToHost, st->stream));
-    check_cuda(cudaMemcpyAsync(hd, dist, (size_t)m * 4, cudaMemcpyDeviceToHost, st->stream));
-    check_cuda(cudaMemcpyAsync(st->h_scalars + 1, st->d_flags, 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 1, st->d_flags + 4, 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 2, wt, 8, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 3, st->d_flags, 4, cudaMemcpyDeviceToHost, st->stream));
     check_cuda(cudaStreamSynchronize(st->stream));
-    if ((uint32_t)st->h_scalars[1] & ERR_INTERNAL) throw Error{GBWT_INTERNAL_ERROR};
-    uint64_t acc = 0;
-    uint32_t cur = 0;                     // ruler 0 is row 0 (rulers are in row order)
-    for (uint32_t it = 0; it < m; it++) {
-        if (it > 0 && cur == 0) throw Error{GBWT_BAD_PARAMETER};   // LF has more than one cycle
-        ho[cur] = (uint32_t)acc;
-        acc += hd[cur];
-        cur = hn[cur];
-    }
-    if (cur != 0 || acc != rows) throw Error{GBWT_BAD_PARAMETER};
-    check_cuda(cudaMemcpyAsync(off, ho, (size_t)m * 4, cudaMemcpyHostToDevice, st->stream));
-    k_walk_emit<<<grid_for(m, 128), 128, 0, st->stream>>>(LF, rul, off, dist, m, cum, n, dT);
+    if ((uint32_t)st->h_scalars[3] & ERR_INTERNAL) throw Error{GBWT_INTERNAL_ERROR};
+    if ((uint32_t)st->h_scalars[1] != 0) throw Error{GBWT_BAD_PARAMETER};
+    // from ruler 0 the whole cycle must come back to row 0 after n+1 steps
+    if (st->h_scalars[2] != (uint64_t)rows) throw Error{GBWT_BAD_PARAMETER};
+    uint32_t *off = slot<uint32_t>(st, S_VAL0, m);
+    k_ruler_off<<<grid_for(m, 256), 256, 0, st->stream>>>(wt, m, off);
+    after_launch(st);
+    k_walk_emit<<<grid_for(m, 128), 128, 0, st->stream>>>(LF, rul, off, m, cum, n, dT);
     after_launch(st);
 }
 
