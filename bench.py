@@ -52,10 +52,13 @@ UNIT = "MB/s"
 WORKLOAD = ("512 MiB repetitive DNA: 4 MiB uniform ACGT base (seed 2), 128 copies with 0.1% substitutions "
             "+ 0.01% indels (length 1-10); PFP W=5 P=16, one text per step")
 
-# Kernel whose launches are timed for the roofline, and its algorithmic
-# bytes per element: the radix-sort scatter reads and writes every key and
-# value once (u64 key + u32 value = 24 B/element on the sort of the parse).
-PROBE_KERNEL = 1   # see gbwt_set_kernel_probe in include/gbwt.h
+# Kernels whose launches are timed for the roofline (gbwt_set_kernel_probe in
+# include/gbwt.h), with the library's algorithmic bytes per launch:
+#   k_seg_sort (the dominant kernel, prefix-doubling rounds sorted inside CTAs):
+#     24 B per active element (read x, group, key; write rank and next entry)
+#   k_rs_downsweep (radix scatter): every key and value read and written once
+PROBE_SEG_SORT = 6
+PROBE_RADIX = 1
 
 
 def log(*a):
@@ -209,7 +212,7 @@ def run_gpu(args):
         st.pfp_bwt_device(dev_text.data_ptr(), dev_out.data_ptr(), n, 5, 16)
     torch.cuda.synchronize()
     stats = st.stats()
-    st.set_kernel_probe(PROBE_KERNEL)
+    st.set_kernel_probe(PROBE_SEG_SORT)
     launches = 0
     barrier()
     torch.cuda.synchronize()
@@ -227,6 +230,13 @@ def run_gpu(args):
     probe = st.stats()
     st.set_kernel_probe(-1)
     clocks = clk.summary()
+
+    # ---- the radix scatter's launches (one extra, untimed step) -------------
+    st.set_kernel_probe(PROBE_RADIX)
+    st.pfp_bwt_device(dev_text.data_ptr(), dev_out.data_ptr(), n, 5, 16)
+    torch.cuda.synchronize()
+    probe_radix = st.stats()
+    st.set_kernel_probe(-1)
 
     # ---- stage breakdown (one extra, untimed step) ------------------------
     st.pfp_bwt_device(dev_text.data_ptr(), dev_out.data_ptr(), n, 5, 16, stage_times=True)
@@ -282,16 +292,10 @@ def run_gpu(args):
     value = ws * n / (ms / 1000.0) / 1e6
     e2e_value = ws * n / (e2e_ms / 1000.0) / 1e6
     peak, peak_kind = measured_peak()
-    roofline = None
-    if probe.get("probe_launches", 0) > 0 and probe.get("probe_ms", 0) > 0:
-        per_launch_bytes = probe["probe_bytes"] / probe["probe_launches"]
-        avg_s = probe["probe_ms"] / probe["probe_launches"] / 1000.0
-        achieved = per_launch_bytes / avg_s / 1e9
-        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": traffic_per_launch(per_launch_bytes),
-                    "kernel": "k_rs_downsweep (radix scatter)", "peak_kind": f"of {peak_kind}",
-                    "launches_timed": probe["probe_launches"], "algorithmic_bytes_per_launch": int(per_launch_bytes),
-                    "share_of_step": round(probe["probe_ms"] / args.steps / ms, 4)}
+    roofline = roofline_of(probe, "k_seg_sort", "k_seg_sort<ParseRem/DictRem> (prefix-doubling rounds in CTAs)",
+                           peak, peak_kind, args.steps, ms)
+    roofline_radix = roofline_of(probe_radix, "k_rs_downsweep", "k_rs_downsweep (radix scatter)", peak, peak_kind,
+                                 1, ms)
     cpu_value, cpu_dt, cpu_n, cpu_threads = cpu_port_sample(text, args.cpu_sample_mib << 20)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -303,6 +307,7 @@ def run_gpu(args):
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": n, "d2h_bytes_per_step": n,
                 "ms_per_step": round(e2e_ms, 3)},
         "roofline": roofline,
+        "roofline_radix": roofline_radix,
         "cpu_baseline": {"value": round(cpu_value, 3), "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": f"first {cpu_n >> 20} MiB of the same text, oracle PFP port, one run "
                                    f"({cpu_dt:.1f} s)"},
@@ -461,16 +466,31 @@ def measure_serving(args, pkg, wl):
     }
 
 
-def traffic_per_launch(per_launch_bytes):
-    """DRAM bytes per launch from the committed ncu capture, scaled to this
-    launch size (bytes per algorithmic byte), or None when absent."""
+def traffic_per_launch(kernel, per_launch_bytes):
+    """DRAM bytes per launch from the committed ncu capture of `kernel`
+    (profiles/traffic.json: DRAM bytes per algorithmic byte), scaled to this
+    launch size, or None when absent."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
-    ratio = d.get("dram_bytes_per_algorithmic_byte")
+    ratio = d.get(kernel, {}).get("dram_bytes_per_algorithmic_byte")
     return None if ratio is None else int(ratio * per_launch_bytes)
+
+
+def roofline_of(probe, key, label, peak, peak_kind, steps, step_ms):
+    """Roofline object from the probe counters of one kernel family."""
+    if probe.get("probe_launches", 0) <= 0 or probe.get("probe_ms", 0) <= 0:
+        return None
+    per_launch_bytes = probe["probe_bytes"] / probe["probe_launches"]
+    avg_s = probe["probe_ms"] / probe["probe_launches"] / 1000.0
+    achieved = per_launch_bytes / avg_s / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic_per_launch(key, per_launch_bytes),
+            "kernel": label, "peak_kind": f"of {peak_kind}", "launches_timed": probe["probe_launches"],
+            "algorithmic_bytes_per_launch": int(per_launch_bytes),
+            "share_of_step": round(probe["probe_ms"] / steps / step_ms, 4)}
 
 
 def main(argv=None):

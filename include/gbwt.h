@@ -256,6 +256,7 @@ int64_t gbwt_server_peak_admitted(void *server);
 #define GBWT_PROBE_PHRASE_HASH      3   /* phrase fingerprint + table insert */
 #define GBWT_PROBE_RUN_FILL         4   /* run blocks written to the output */
 #define GBWT_PROBE_MIXED_SCATTER    5   /* mixed-block bytes scattered      */
+#define GBWT_PROBE_SEG_SORT         6   /* prefix-doubling round, CTA groups */
 
 /*
  * Starts timing every launch of one kernel family (GBWT_PROBE_*) on the

@@ -108,6 +108,7 @@ PROBE_TRIGGER_SCAN = 2
 PROBE_PHRASE_HASH = 3
 PROBE_RUN_FILL = 4
 PROBE_MIXED_SCATTER = 5
+PROBE_SEG_SORT = 6
 
 
 def _lib() -> ctypes.CDLL:

@@ -344,7 +344,7 @@ extern "C" int64_t gbwt_pfp_parse(void *storage, const uint8_t *T, int64_t n, in
 extern "C" int64_t gbwt_set_kernel_probe(void *storage, int32_t kernel)
 {
     Storage *st = (Storage *)storage;
-    if (!st || kernel < -1 || kernel > GBWT_PROBE_MIXED_SCATTER) return GBWT_BAD_PARAMETER;
+    if (!st || kernel < -1 || kernel > GBWT_PROBE_SEG_SORT) return GBWT_BAD_PARAMETER;
     return guarded([&]() -> int64_t {
         if (kernel >= 0 && !st->probe_ev) {
             const int cap = 1024;

@@ -420,23 +420,84 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         const uint32_t ss = s_ss[sg], se = s_ss[sg + 1], s = se - ss;
         const uint32_t g = s_sg[sg];
         uint64_t *key = s_key + ss;
-        // Fast paths for groups whose isa[x+h] takes one or two values (most
-        // groups of a repetitive text in early rounds): a stable partition
-        // in input order replaces the sort.
-        uint32_t mn = 0xFFFFFFFFu, mx = 0;
+        // Fast paths (groups of a repetitive text's copies): the next ranks
+        // isa[x+h] of a group usually take one value, two values, or one
+        // majority value with a few outliers.  A stable partition in input
+        // order replaces the sort.  One counting pass first: min, max, and
+        // for two candidate values (middle and first member) their counts
+        // and the number of members below them.
+        const uint32_t c1 = (uint32_t)(key[s >> 1] >> 32), c2 = (uint32_t)(key[0] >> 32);
+        uint32_t mn = 0xFFFFFFFFu, mx = 0, n1 = 0, n2 = 0, b1 = 0, b2 = 0;
         for (uint32_t c0 = 0; c0 < s; c0 += 32) {
             const uint32_t i = c0 + lane;
-            if (i < s) {
-                const uint32_t k2 = (uint32_t)(key[i] >> 32);
+            const bool in = i < s;
+            const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : c1;
+            if (in) {
                 mn = min(mn, k2);
                 mx = max(mx, k2);
             }
+            n1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c1));
+            n2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c2));
+            b1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c1));
+            b2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c2));
         }
         mn = __reduce_min_sync(0xFFFFFFFFu, mn);
         mx = __reduce_max_sync(0xFFFFFFFFu, mx);
-        bool two = mn != mx;
+        const uint32_t mj = n1 >= n2 ? c1 : c2, ne = n1 >= n2 ? n1 : n2, nl = n1 >= n2 ? b1 : b2;
+        if (collect_stats && lane == 0)
+            atomicAdd(flags + 20 + (mn == mx ? 0 : (s - ne <= 32 ? 3 : 2)), s);
+        if (s <= SS_WARPMAX && s - ne <= 32) {
+            // majority members in input order after the nl smaller ones;
+            // outlier j goes to lane j and is ranked by counting
+            uint64_t mine = ~0ull;
+            uint32_t no = 0, re = 0;
+            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+                const uint32_t i = c0 + lane;
+                const bool in = i < s;
+                const uint64_t kk = in ? key[i] : 0ull;
+                const bool me = in && (uint32_t)(kk >> 32) == mj;
+                const unsigned be = __ballot_sync(0xFFFFFFFFu, me);
+                const unsigned bo = __ballot_sync(0xFFFFFFFFu, in && !me);
+                if (me) {
+                    const uint32_t pos = nl + re + __popc(be & ((1u << lane) - 1u));
+                    const uint32_t li = (uint32_t)kk & 0xFFFFu;
+                    const bool done = ne == 1 || rem(s_x[li]) <= h2;
+                    s_nh[ss + pos] = (g + nl) | (done ? 0x80000000u : 0u);
+                    s_perm[ss + pos] = (uint16_t)li;
+                }
+                re += __popc(be);
+                if (bo) {
+                    const uint32_t want = lane - no;      // this chunk's outlier for this lane
+                    const bool take = lane >= no && want < (uint32_t)__popc(bo);
+                    const uint32_t src = take ? (uint32_t)__fns(bo, 0, (int)want + 1) : lane;
+                    const uint64_t got = __shfl_sync(0xFFFFFFFFu, kk, src);
+                    if (take) mine = got;
+                    no += __popc(bo);
+                }
+            }
+            const uint32_t my2 = (uint32_t)(mine >> 32);
+            uint32_t rk = 0, lt2 = 0, eq2 = 0;
+            for (uint32_t q = 0; q < no; q++) {
+                const uint64_t o = __shfl_sync(0xFFFFFFFFu, mine, q);
+                const uint32_t o2 = (uint32_t)(o >> 32);
+                rk += o < mine;
+                lt2 += o2 < my2;
+                eq2 += o2 == my2;
+            }
+            if (lane < no) {
+                const bool above = my2 > mj;
+                const uint32_t pos = above ? rk + ne : rk;
+                const uint32_t li = (uint32_t)mine & 0xFFFFu;
+                const bool done = eq2 == 1 || rem(s_x[li]) <= h2;
+                s_nh[ss + pos] = (g + (above ? lt2 + ne : lt2)) | (done ? 0x80000000u : 0u);
+                s_perm[ss + pos] = (uint16_t)li;
+            }
+            continue;
+        }
+        // exactly two values, both frequent: stable two-way partition
+        bool two = false;
         uint32_t cmn = 0;                    // members with the smaller value
-        if (two) {
+        {
             bool other = false;
             for (uint32_t c0 = 0; c0 < s; c0 += 32) {
                 const uint32_t i = c0 + lane;
@@ -446,7 +507,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
             }
             two = !__any_sync(0xFFFFFFFFu, other);
         }
-        if (mn == mx || two) {
+        if (two) {
             uint32_t rmn = 0, rmx = 0;       // running ranks among equal members
             for (uint32_t c0 = 0; c0 < s; c0 += 32) {
                 const uint32_t i = c0 + lane;
@@ -459,7 +520,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
                     const uint32_t li = (uint32_t)key[i] & 0xFFFFu;
                     uint32_t pos, nh;
                     bool single;
-                    if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = (mn == mx ? s : cmn) == 1; }
+                    if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = cmn == 1; }
                     else { pos = cmn + rmx + __popc(bhi & lt); nh = g + cmn; single = s - cmn == 1; }
                     const bool done = single || rem(s_x[li]) <= h2;
                     s_nh[ss + pos] = nh | (done ? 0x80000000u : 0u);
@@ -518,9 +579,11 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         const uint32_t v = s_nh[p];
         const uint32_t nh = v & 0x7FFFFFFFu;
         const uint32_t x = s_x[s_perm[p]];
-        isa[x] = nh;
+        const uint32_t sg = s_seg[p];                 // slots stay inside their group
+        // isa[x] already holds the old group head (the rank it was made
+        // active with); only a changed rank is written
+        if (nh != s_sg[sg]) isa[x] = nh;
         if (v >> 31) {
-            const uint32_t sg = s_seg[p];
             sa[s_sg[sg] + (p - s_ss[sg])] = x;
         } else {
             out_x[base + apre] = x;
@@ -583,16 +646,22 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         if (!big) {
             uint32_t *counter = (uint32_t *)st->d_scalars;
             check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-            if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 4 * sizeof(uint32_t), st->stream));
+            if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 8 * sizeof(uint32_t), st->stream));
+            probe_begin(st, GBWT_PROBE_SEG_SORT);
             k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
                 act_x, act_g, key2, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags, debug);
+            // per active element: read x, group, key (12 B); write its rank and
+            // either its next-round (x, group) or its final suffix-array slot (12 B)
+            probe_end(st, GBWT_PROBE_SEG_SORT, 24ull * A);
             after_launch(st);
             fetch_scalars(st, 1);
             if (debug) {
-                uint32_t tiers[4];
+                uint32_t tiers[8];
                 check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
                 fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
                         SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
+                fprintf(stderr, "gbwt:   larger groups: one value %u, majority + <=32 outliers %u, other %u\n",
+                        tiers[4], tiers[7], tiers[6]);
             }
             A = (uint32_t)st->h_scalars[0];
             uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
