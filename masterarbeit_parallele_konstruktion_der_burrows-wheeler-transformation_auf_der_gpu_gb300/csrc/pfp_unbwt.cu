@@ -87,14 +87,18 @@ __global__ void __launch_bounds__(RS_THREADS) k_lf_rank(const uint8_t *__restric
     }
 #pragma unroll
     for (int q = 0; q < RS_ITEMS; q++) {
+        // the lowest lane of each digit class reads and advances the warp's
+        // counter; the others take the old value from it
         const uint32_t d = dg[q];
-        const bool valid = d != 0xFFFFFFFFu;
-        const uint32_t dd = valid ? d : 0u;
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        const uint32_t prior = wh[dd];
-        __syncwarp();
+        const unsigned leader = (unsigned)(__ffs(peers) - 1);
+        uint32_t prior = 0;
+        if (lane == leader && d != 0xFFFFFFFFu) {
+            prior = wh[d];
+            wh[d] = prior + (uint32_t)__popc(peers);
+        }
+        prior = __shfl_sync(0xFFFFFFFFu, prior, leader);
         rk[q] = prior + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-        if (valid) wh[dd] = prior + (uint32_t)__popc(peers);
         __syncwarp();
     }
     __syncthreads();
