@@ -193,6 +193,28 @@ int64_t gbwt_libcubwt_unbwt(void *storage, const uint8_t *T, uint8_t *U, int64_t
 int64_t gbwt_get_stats(void *storage, gbwt_stats *out);
 
 /*
+ * Tuning knobs of a storage object (0 = built-in default).  They change how
+ * the work is scheduled, never the result.  No counterpart in the reference
+ * (its launch shapes are compile-time constants); an autotuner picks them
+ * per size class (package module autotune).
+ */
+typedef struct gbwt_tuning {
+    int32_t hash_log2_max;      /* phrase hash table: at most 2^k slots (16..28; default 22)        */
+    int32_t batch_seg_tiles;    /* batch: texts grouped until a sort segment holds this many
+                                   4096-element tiles (1..1024; default 8)                           */
+    int32_t batch_pad_eighths;  /* batch: one text per segment when tile padding is at most this
+                                   many eighths of the elements (0..64; default 1)                   */
+    int32_t batch_radix_bits;   /* batch output sort digit width: 8, 9, or 0 = fewest passes         */
+    int32_t unbwt_rate_log2;    /* inverse BWT: one ruler per 2^k rows (2..12; default 7)            */
+    int32_t reserved[3];
+} gbwt_tuning;
+
+/* Sets (t != NULL) or resets (t == NULL) the storage's tuning. */
+int64_t gbwt_set_tuning(void *storage, const gbwt_tuning *t);
+/* Checks a tuning without a storage object: GBWT_NO_ERROR or GBWT_BAD_PARAMETER. */
+int64_t gbwt_check_tuning(const gbwt_tuning *t);
+
+/*
  * Frees the storage's scratch (it grows again on the next call).  No
  * counterpart in the reference, whose device buffers are globals freed ad
  * hoc (K:36-98); used by the serving loop to return memory to its budget.

@@ -13,6 +13,7 @@ raises ``GbwtLibraryMissing``.
 from __future__ import annotations
 
 import ctypes
+import json
 import os
 from dataclasses import dataclass
 
@@ -90,8 +91,54 @@ EXPORTS = (
     "gbwt_write_out_txt", "gbwt_free_host", "gbwt_error_string", "gbwt_set_kernel_probe",
     "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch", "gbwt_trim_device_storage",
     "gbwt_server_create", "gbwt_server_destroy", "gbwt_submit", "gbwt_poll", "gbwt_wait", "gbwt_server_drain",
-    "gbwt_server_peak_admitted", "gbwt_unbwt", "gbwt_libcubwt_unbwt",
+    "gbwt_server_peak_admitted", "gbwt_unbwt", "gbwt_libcubwt_unbwt", "gbwt_set_tuning", "gbwt_check_tuning",
 )
+
+TUNING_KNOBS = ("hash_log2_max", "batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits", "unbwt_rate_log2")
+
+
+class Tuning(ctypes.Structure):
+    """gbwt_tuning (include/gbwt.h): scheduling knobs, 0 = default."""
+    _fields_ = [(k, ctypes.c_int32) for k in TUNING_KNOBS] + [("reserved", ctypes.c_int32 * 3)]
+
+    @classmethod
+    def from_dict(cls, d: dict | None) -> "Tuning":
+        t = cls()
+        for k, v in (d or {}).items():
+            if k not in TUNING_KNOBS:
+                raise ValueError(f"unknown tuning knob {k}")
+            setattr(t, k, int(v))
+        return t
+
+
+def check_tuning(d: dict) -> bool:
+    """True when the C library accepts these knob values (no GPU needed)."""
+    t = Tuning.from_dict(d)
+    return _lib().gbwt_check_tuning(ctypes.byref(t)) == 0
+
+
+TUNING_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+
+
+def load_tuning(path: str | None = None) -> dict | None:
+    """Size classes written by the autotuner ({"classes": {"<MiB>": {knob: value}}}), or None."""
+    p = path or os.environ.get("GBWT_TUNING", TUNING_FILE)
+    if not p or not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
+def tuning_for(n: int, table: dict | None) -> dict | None:
+    """The knobs of the largest size class not above n bytes (the smallest class for smaller n)."""
+    if not table or not table.get("classes"):
+        return None
+    classes = sorted((int(k), v) for k, v in table["classes"].items())
+    best = classes[0][1]
+    for mib, knobs in classes:
+        if (mib << 20) <= n:
+            best = knobs
+    return best
 
 
 class JobInfo(ctypes.Structure):
@@ -149,6 +196,10 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_libcubwt_bwt.restype = i64
     L.gbwt_pfp_bwt_batch.argtypes = [vp, u8p, ctypes.c_void_p, i32, u8p, i32, i32, u32]
     L.gbwt_pfp_bwt_batch.restype = i64
+    L.gbwt_set_tuning.argtypes = [vp, ctypes.c_void_p]
+    L.gbwt_set_tuning.restype = i64
+    L.gbwt_check_tuning.argtypes = [ctypes.c_void_p]
+    L.gbwt_check_tuning.restype = i64
     L.gbwt_unbwt.argtypes = [vp, u8p, u8p, i64, i64, u32]
     L.gbwt_unbwt.restype = i64
     L.gbwt_libcubwt_unbwt.argtypes = [vp, u8p, u8p, i64, ctypes.c_void_p, i32]
@@ -189,10 +240,33 @@ class Storage:
     """Device storage (stream + scratch pools), libcubwt_allocate_device_storage
     style (libcubwt.cuh:48-59).  Use one per thread; reuse across calls."""
 
-    def __init__(self, max_length: int = 0):
+    def __init__(self, max_length: int = 0, tuning="auto"):
+        """tuning: "auto" applies the autotuner's size classes (tuning.json, if
+        present) to every call; a dict of knobs fixes them; None = defaults."""
         self._p = ctypes.c_void_p()
         _check(_lib().gbwt_allocate_device_storage(ctypes.byref(self._p), int(max_length)),
                "gbwt_allocate_device_storage")
+        self._table = load_tuning() if tuning == "auto" else None
+        self._applied = None
+        if isinstance(tuning, dict):
+            self._set_raw(tuning)
+
+    def _set_raw(self, knobs: dict | None) -> None:
+        t = Tuning.from_dict(knobs) if knobs else None
+        _check(_lib().gbwt_set_tuning(self.handle, ctypes.byref(t) if t is not None else None), "gbwt_set_tuning")
+
+    def set_tuning(self, knobs: dict | None) -> None:
+        """Fixes the tuning knobs (None = defaults); size classes no longer apply."""
+        self._table = None
+        self._set_raw(knobs)
+
+    def _auto(self, n: int) -> None:
+        if self._table is None:
+            return
+        knobs = tuning_for(int(n), self._table)
+        if knobs is not self._applied:
+            self._set_raw(knobs)
+            self._applied = knobs
 
     @property
     def handle(self) -> ctypes.c_void_p:
@@ -231,6 +305,7 @@ class Storage:
         t = _host_u8(text)
         out = np.empty(max(len(t), 1), dtype=np.uint8)
         flags = (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (FLAG_STAGE_TIMES if stage_times else 0)
+        self._auto(len(t))
         _check(_lib().gbwt_pfp_bwt(self.handle, t.ctypes.data, out.ctypes.data, len(t), W, P, flags),
                "gbwt_pfp_bwt")
         return out[:len(t)]
@@ -242,6 +317,7 @@ class Storage:
                 or not out.flags.c_contiguous or len(out) < len(text):
             raise ValueError("text/out must be contiguous uint8 arrays, len(out) >= len(text)")
         flags = FLAG_SMALL_ALPHABET if small_alphabet else 0
+        self._auto(len(text))
         return _check(_lib().gbwt_pfp_bwt(self.handle, text.ctypes.data, out.ctypes.data, len(text), W, P, flags),
                       "gbwt_pfp_bwt")
 
@@ -265,6 +341,7 @@ class Storage:
                 or len(concat) < offsets[-1]:
             raise ValueError("concat/out must be contiguous uint8 arrays covering offsets[-1] bytes")
         flags = (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (FLAG_STAGE_TIMES if stage_times else 0)
+        self._auto(int(offsets[-1]))
         return _check(_lib().gbwt_pfp_bwt_batch(self.handle, concat.ctypes.data, offsets.ctypes.data,
                                                 len(offsets) - 1, out.ctypes.data, W, P, flags),
                       "gbwt_pfp_bwt_batch")
@@ -275,6 +352,7 @@ class Storage:
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         flags = FLAG_DEVICE_POINTERS | (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (
             FLAG_STAGE_TIMES if stage_times else 0)
+        self._auto(int(offsets[-1]))
         return _check(_lib().gbwt_pfp_bwt_batch(self.handle, ctypes.c_void_p(text_ptr), offsets.ctypes.data,
                                                 len(offsets) - 1, ctypes.c_void_p(out_ptr), W, P, flags),
                       "gbwt_pfp_bwt_batch")
@@ -292,10 +370,12 @@ class Storage:
         """Inverse BWT on the GPU of gbwt_pfp_bwt's output and its primary index."""
         b = _host_u8(L)
         T = np.empty(max(len(b), 1), dtype=np.uint8)
+        self._auto(len(b))
         _check(_lib().gbwt_unbwt(self.handle, b.ctypes.data, T.ctypes.data, len(b), int(primary), 0), "gbwt_unbwt")
         return T[:len(b)]
 
     def unbwt_device(self, L_ptr: int, T_ptr: int, n: int, primary: int) -> int:
+        self._auto(n)
         return _check(_lib().gbwt_unbwt(self.handle, ctypes.c_void_p(L_ptr), ctypes.c_void_p(T_ptr), n, int(primary),
                                         FLAG_DEVICE_POINTERS), "gbwt_unbwt")
 
@@ -316,6 +396,7 @@ class Storage:
         """Device-pointer variant: ``text_ptr``/``out_ptr`` are CUDA device addresses."""
         flags = FLAG_DEVICE_POINTERS | (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (
             FLAG_STAGE_TIMES if stage_times else 0)
+        self._auto(n)
         return _check(_lib().gbwt_pfp_bwt(self.handle, ctypes.c_void_p(text_ptr), ctypes.c_void_p(out_ptr), n, W, P,
                                           flags), "gbwt_pfp_bwt")
 

@@ -477,6 +477,31 @@ extern "C" int64_t gbwt_get_stats(void *storage, gbwt_stats *out)
     return GBWT_NO_ERROR;
 }
 
+extern "C" int64_t gbwt_check_tuning(const gbwt_tuning *t)
+{
+    if (!t) return GBWT_BAD_PARAMETER;
+    const bool ok = (t->hash_log2_max == 0 || (t->hash_log2_max >= 16 && t->hash_log2_max <= 28)) &&
+                    (t->batch_seg_tiles >= 0 && t->batch_seg_tiles <= 1024) &&
+                    (t->batch_pad_eighths >= 0 && t->batch_pad_eighths <= 64) &&
+                    (t->batch_radix_bits == 0 || t->batch_radix_bits == 8 || t->batch_radix_bits == 9) &&
+                    (t->unbwt_rate_log2 == 0 || (t->unbwt_rate_log2 >= 2 && t->unbwt_rate_log2 <= 12));
+    return ok ? GBWT_NO_ERROR : GBWT_BAD_PARAMETER;
+}
+
+extern "C" int64_t gbwt_set_tuning(void *storage, const gbwt_tuning *t)
+{
+    Storage *st = (Storage *)storage;
+    if (!st) return GBWT_BAD_PARAMETER;
+    if (!t) {
+        st->tuning = gbwt_tuning{};
+        return GBWT_NO_ERROR;
+    }
+    const int64_t rc = gbwt_check_tuning(t);
+    if (rc != GBWT_NO_ERROR) return rc;
+    st->tuning = *t;
+    return GBWT_NO_ERROR;
+}
+
 extern "C" int64_t gbwt_trim_device_storage(void *storage)
 {
     Storage *st = (Storage *)storage;

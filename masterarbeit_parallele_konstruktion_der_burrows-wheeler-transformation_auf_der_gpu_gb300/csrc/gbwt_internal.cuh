@@ -49,6 +49,7 @@ struct Storage {
     uint64_t *d_scalars = nullptr;      // device scalars (64 entries)
     uint32_t *h_meta = nullptr;         // pinned batch layout (grows on demand)
     size_t h_meta_cap = 0;
+    gbwt_tuning tuning = {};            // 0 = default for every knob
     gbwt_stats stats;
     int64_t launches = 0;
     bool stage_times = false;
@@ -135,6 +136,12 @@ inline unsigned grid_for(size_t n, unsigned per_block)
     size_t g = (n + per_block - 1) / per_block;
     return (unsigned)(g ? g : 1);
 }
+
+// Effective tuning values (defaults for 0).
+inline int tune_hash_log2(const Storage *st) { return st->tuning.hash_log2_max ? st->tuning.hash_log2_max : 22; }
+inline int tune_seg_tiles(const Storage *st) { return st->tuning.batch_seg_tiles ? st->tuning.batch_seg_tiles : 8; }
+inline int tune_pad_eighths(const Storage *st) { return st->tuning.batch_pad_eighths ? st->tuning.batch_pad_eighths : 1; }
+inline int tune_unbwt_rate_log2(const Storage *st) { return st->tuning.unbwt_rate_log2 ? st->tuning.unbwt_rate_log2 : 7; }
 
 inline int bits_for(uint64_t v)   // bits needed to represent values in [0, v]
 {

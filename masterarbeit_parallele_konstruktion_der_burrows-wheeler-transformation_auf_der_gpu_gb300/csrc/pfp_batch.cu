@@ -103,7 +103,6 @@ struct StoreTid {
 // segmented stable radix sort then leaves each text's elements in its BWT
 // order, padding (all-ones keys) at the segment ends.
 // ---------------------------------------------------------------------
-constexpr uint32_t SEG_MIN = 8u * RS_TILE;
 
 struct BatchLayout {
     uint32_t k = 0;                 // non-empty texts
@@ -233,9 +232,9 @@ __global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, 
 }
 
 // Host layout of a batch: the non-empty texts in X, and the segments.  One
-// text per segment when its tile padding costs at most 1/8 of the elements
-// (the key then needs no text bits); otherwise texts are grouped until a
-// segment holds SEG_MIN elements.
+// text per segment when the tile padding costs at most pad_eighths / 8 of
+// the elements (the key then needs no text bits); otherwise texts are
+// grouped until a segment holds seg_tiles tiles (tuning knobs).
 static BatchLayout batch_layout(Storage *st, const int64_t *offsets, int32_t k, int W)
 {
     BatchLayout bl;
@@ -247,7 +246,9 @@ static BatchLayout batch_layout(Storage *st, const int64_t *offsets, int32_t k, 
         if (!len) continue;
         single_tiles += (len + RS_TILE - 1) / RS_TILE;
     }
-    const uint64_t seg_min = single_tiles * RS_TILE <= bl.total + bl.total / 8 ? 1u : SEG_MIN;
+    const uint64_t pad = (uint64_t)tune_pad_eighths(st);
+    const uint64_t seg_min = single_tiles * RS_TILE <= bl.total + bl.total * pad / 8
+                                 ? 1u : (uint64_t)tune_seg_tiles(st) * RS_TILE;
     for (int32_t t = 0; t < k; t++) {
         const uint64_t len = (uint64_t)(offsets[t + 1] - offsets[t]);
         if (!len) continue;
@@ -340,7 +341,9 @@ static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dme
     // 4096-key tiles' histograms (and their scan) too large.
     const int sb = tlb + gb;
     uint32_t *nv = nullptr, *nv2 = nullptr;
-    if ((sb + 8) / 9 < (sb + 7) / 8) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    const int want = st->tuning.batch_radix_bits;
+    const bool nine = want ? want == 9 : (sb + 8) / 9 < (sb + 7) / 8;
+    if (nine) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     stage_mark(st, 5);
     k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,

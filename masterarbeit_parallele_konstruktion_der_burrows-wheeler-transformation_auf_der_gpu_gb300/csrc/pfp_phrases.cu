@@ -252,7 +252,8 @@ void run_phrases(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph,
     uint32_t *slot_of = slot<uint32_t>(st, S_SLOT, z);
     uint32_t *isrep = slot<uint32_t>(st, S_PID, z);     // reused for pid below
     const uint32_t full_c = pow2_at_least((uint64_t)z * 2);
-    uint32_t c = full_c < (1u << 22) ? full_c : (1u << 22);
+    const uint32_t cap = 1u << tune_hash_log2(st);       // L2-sized table while the dictionary fits
+    uint32_t c = full_c < cap ? full_c : cap;
     uint64_t seed = 0x2545F4914F6CDD1Dull;
     uint32_t d = 0;
     uint32_t *tdense = nullptr, *dlen = nullptr, *dstart = nullptr;

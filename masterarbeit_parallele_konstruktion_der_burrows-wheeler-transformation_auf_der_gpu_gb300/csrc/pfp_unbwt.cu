@@ -239,10 +239,12 @@ void pfp_to_libcubwt(Storage *st, const uint8_t *dO, uint32_t n, uint32_t p, uin
 void run_unbwt(Storage *st, const uint8_t *dLc, uint32_t n, uint32_t i, uint8_t *dT)
 {
     const uint32_t rows = n + 1u;
-    // ~1/128 of the rows are rulers: the longest walk (about 128 ln m steps of
-    // one dependent load each) sets the time of both walk passes
-    uint32_t rate = 16;
-    while (rate < 128 && (uint64_t)rate * 65536u < rows) rate <<= 1;
+    // ~1/128 of the rows are rulers (tuning knob): the longest walk (about
+    // rate * ln m steps of one dependent load each) sets the time of both
+    // walk passes; small inputs use denser rulers
+    const uint32_t rate_max = 1u << tune_unbwt_rate_log2(st);
+    uint32_t rate = 4;
+    while (rate < rate_max && (uint64_t)rate * 65536u < rows) rate <<= 1;
     const uint32_t rate_mask = rate - 1u;
     // rulers in row order
     check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
