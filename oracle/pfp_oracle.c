@@ -63,31 +63,119 @@ static uint8_t *make_enlarged(const uint8_t *T, int64_t n, int W)
 /* D receives the window's last position; n+W-1 is appended last.        */
 /* D needs room for max(n-W+1,0)+1 entries.  Returns z = |D|.           */
 /* ------------------------------------------------------------------ */
+static int is_trigger(const uint8_t *T, int64_t s, int W, int P)
+{
+    int pot = 1, res = 0, equal = 1, i;
+    for (i = W - 1; i >= 0; i--) {                  /* K:468-473 */
+        if (equal && T[s + i] != T[i]) equal = 0;
+        res = (res + pot * (int)T[s + i]) % P;
+        pot = (pot * 2) % P;
+    }
+    return s > 0 && (res == 0 || equal);            /* K:475 */
+}
+
 int64_t gbo_trigger_scan(const uint8_t *T, int64_t n, int W, int P, int64_t *D)
 {
+    const int64_t nw = n - W + 1 > 0 ? n - W + 1 : 0;    /* windows s with s+W-1 < n */
     int64_t z = 0, s;
-    for (s = 0; s + W - 1 < n; s++) {
-        int pot = 1, res = 0, equal = 1, i;
-        for (i = W - 1; i >= 0; i--) {              /* K:468-473 */
-            if (equal && T[s + i] != T[i]) equal = 0;
-            res = (res + pot * (int)T[s + i]) % P;
-            pot = (pot * 2) % P;
+#ifdef _OPENMP
+    if (nw > (1 << 20)) {
+        /* windows are independent: count per chunk, then write at the chunk's offset */
+        extern int omp_get_max_threads(void);
+        const int64_t nch = 8 * (int64_t)omp_get_max_threads();
+        int64_t *cnt = (int64_t *)calloc((size_t)nch + 1, sizeof(int64_t)), c;
+        if (cnt) {
+#pragma omp parallel for schedule(dynamic)
+            for (c = 0; c < nch; c++) {
+                int64_t k = 0, q;
+                for (q = c * nw / nch; q < (c + 1) * nw / nch; q++) k += is_trigger(T, q, W, P);
+                cnt[c + 1] = k;
+            }
+            for (c = 0; c < nch; c++) cnt[c + 1] += cnt[c];
+#pragma omp parallel for schedule(dynamic)
+            for (c = 0; c < nch; c++) {
+                int64_t k = cnt[c], q;
+                for (q = c * nw / nch; q < (c + 1) * nw / nch; q++)
+                    if (is_trigger(T, q, W, P)) D[k++] = q + W - 1;
+            }
+            z = cnt[nch];
+            free(cnt);
+            D[z++] = n + W - 1;                          /* K:573-576 */
+            return z;
         }
-        if (s > 0 && (res == 0 || equal))            /* K:475 */
-            D[z++] = s + W - 1;
     }
+#endif
+    for (s = 0; s < nw; s++)
+        if (is_trigger(T, s, W, P)) D[z++] = s + W - 1;
     D[z++] = n + W - 1;                              /* K:573-576 */
     return z;
 }
 
 /* ------------------------------------------------------------------ */
 /* Generic stable merge sort with a context comparator (qsort has none). */
+/* With OpenMP the two halves sort as tasks and large merges split by    */
+/* divide and conquer (a pivot from the left run, its lower bound in the */
+/* right run); the order is the same as the sequential stable sort.      */
 /* ------------------------------------------------------------------ */
 typedef int (*cmp_fn)(int64_t a, int64_t b, const void *ctx);
 
+#define MS_PAR_MIN (1 << 15)
+
+/* Stable merge of the sorted runs a[l1..r1) (first) and a[l2..r2) into   */
+/* out[o..).  Large merges split at a pivot of the longer run: elements   */
+/* of the other run that must precede it (strictly smaller when the pivot */
+/* is from the first run, not larger when from the second) go left.      */
+static void merge2(const int64_t *a, int64_t l1, int64_t r1, int64_t l2, int64_t r2, int64_t *out, int64_t o,
+                   cmp_fn cmp, const void *ctx)
+{
+    const int64_t n1 = r1 - l1, n2 = r2 - l2;
+    if (n1 + n2 > MS_PAR_MIN && n1 > 0 && n2 > 0) {
+        int64_t i, j, lo, hi;
+        if (n1 >= n2) {
+            i = l1 + n1 / 2;                      /* pivot from the first run */
+            lo = l2; hi = r2;
+            while (lo < hi) {
+                const int64_t m = lo + (hi - lo) / 2;
+                if (cmp(a[m], a[i], ctx) < 0) lo = m + 1; else hi = m;
+            }
+            j = lo;
+            out[o + (i - l1) + (j - l2)] = a[i];
+#ifdef _OPENMP
+#pragma omp task if ((i - l1) + (j - l2) > MS_PAR_MIN)
+#endif
+            merge2(a, l1, i, l2, j, out, o, cmp, ctx);
+            merge2(a, i + 1, r1, j, r2, out, o + (i - l1) + (j - l2) + 1, cmp, ctx);
+        } else {
+            j = l2 + n2 / 2;                      /* pivot from the second run */
+            lo = l1; hi = r1;
+            while (lo < hi) {
+                const int64_t m = lo + (hi - lo) / 2;
+                if (cmp(a[j], a[m], ctx) < 0) hi = m; else lo = m + 1;
+            }
+            i = lo;                               /* first-run elements not larger go first */
+            out[o + (i - l1) + (j - l2)] = a[j];
+#ifdef _OPENMP
+#pragma omp task if ((i - l1) + (j - l2) > MS_PAR_MIN)
+#endif
+            merge2(a, l1, i, l2, j, out, o, cmp, ctx);
+            merge2(a, i, r1, j + 1, r2, out, o + (i - l1) + (j - l2) + 1, cmp, ctx);
+        }
+#ifdef _OPENMP
+#pragma omp taskwait
+#endif
+        return;
+    }
+    {
+        int64_t p = l1, q = l2, k = o;
+        while (p < r1 && q < r2) out[k++] = (cmp(a[q], a[p], ctx) < 0) ? a[q++] : a[p++];
+        while (p < r1) out[k++] = a[p++];
+        while (q < r2) out[k++] = a[q++];
+    }
+}
+
 static void msort_rec(int64_t *a, int64_t *tmp, int64_t lo, int64_t hi, cmp_fn cmp, const void *ctx)
 {
-    int64_t mid, i, j, k;
+    int64_t mid, i, j;
     if (hi - lo < 24) {                              /* insertion sort */
         for (i = lo + 1; i < hi; i++) {
             int64_t v = a[i];
@@ -98,13 +186,16 @@ static void msort_rec(int64_t *a, int64_t *tmp, int64_t lo, int64_t hi, cmp_fn c
         return;
     }
     mid = lo + (hi - lo) / 2;
+#ifdef _OPENMP
+#pragma omp task shared(a, tmp) if (hi - lo > MS_PAR_MIN)
+#endif
     msort_rec(a, tmp, lo, mid, cmp, ctx);
     msort_rec(a, tmp, mid, hi, cmp, ctx);
+#ifdef _OPENMP
+#pragma omp taskwait
+#endif
     if (cmp(a[mid - 1], a[mid], ctx) <= 0) return;
-    i = lo; j = mid; k = lo;
-    while (i < mid && j < hi) tmp[k++] = (cmp(a[j], a[i], ctx) < 0) ? a[j++] : a[i++];
-    while (i < mid) tmp[k++] = a[i++];
-    while (j < hi) tmp[k++] = a[j++];
+    merge2(a, lo, mid, mid, hi, tmp, lo, cmp, ctx);
     memcpy(a + lo, tmp + lo, (size_t)(hi - lo) * sizeof(int64_t));
 }
 
@@ -114,7 +205,14 @@ static int msort(int64_t *a, int64_t n, cmp_fn cmp, const void *ctx)
     if (n < 2) return 0;
     tmp = (int64_t *)malloc((size_t)n * sizeof(int64_t));
     if (!tmp) return -1;
-    msort_rec(a, tmp, 0, n, cmp, ctx);
+#ifdef _OPENMP
+    if (n > MS_PAR_MIN) {
+#pragma omp parallel
+#pragma omp single
+        msort_rec(a, tmp, 0, n, cmp, ctx);
+    } else
+#endif
+        msort_rec(a, tmp, 0, n, cmp, ctx);
     free(tmp);
     return 0;
 }
@@ -271,10 +369,11 @@ int gbo_pfp_bwt_ex(const uint8_t *T, int64_t n, int W, int P, int small_alphabet
                    uint8_t *L, gbo_stats *st, int64_t *meta_out, int64_t *parse_sa_out)
 {
     int rc = 0;
-    int64_t z = 0, k, j, c_i, s_n = 0, out = 0, max_len = 0, mixed = 0, mixed_elems = 0;
+    int64_t z = 0, k, j, c_i, s_n = 0, max_len = 0, mixed = 0, mixed_elems = 0;
     uint8_t *X = NULL;
     int64_t *D = NULL, *start = NULL, *len = NULL, *order = NULL, *meta = NULL, *sa = NULL;
     int64_t *next_rank = NULL, *colex = NULL, *Lv = NULL, *s_idx = NULL, *blk = NULL, *dcount = NULL;
+    int64_t *hi_of = NULL, *boff = NULL, max_blk = 0;
     s_entry *S = NULL;
     pctx c;
 
@@ -316,27 +415,33 @@ int gbo_pfp_bwt_ex(const uint8_t *T, int64_t n, int W, int P, int small_alphabet
     for (k = 0; k < z; k++) colex[k] = k;
     if (msort(colex, z, cmp_colex, &c)) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
 
-    /* L values and S (K:2509-2592) */
+    /* L values and S (K:2509-2592); blk[c_i] first holds the S offset of c_i */
+    blk = (int64_t *)malloc((size_t)(z + 1) * sizeof(int64_t));
+    if (!blk) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
     Lv[0] = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
     for (c_i = 1; c_i < z; c_i++) {
         int64_t a = colex[c_i], b = colex[c_i - 1], l = 0;
         while (l < len[a] && l < len[b] && X[D[a] - l] == X[D[b] - l]) l++;
         Lv[c_i] = l;
     }
+    blk[0] = 0;
     for (c_i = 0; c_i < z; c_i++) {
         int64_t lo = Lv[c_i] > W ? Lv[c_i] : W;
-        if (len[colex[c_i]] > lo) s_n += len[colex[c_i]] - lo;
+        blk[c_i + 1] = blk[c_i] + (len[colex[c_i]] > lo ? len[colex[c_i]] - lo : 0);
     }
+    s_n = blk[z];
     S = (s_entry *)malloc((size_t)(s_n ? s_n : 1) * sizeof(s_entry));
     s_idx = (int64_t *)malloc((size_t)(s_n ? s_n : 1) * sizeof(int64_t));
-    blk = (int64_t *)malloc((size_t)(z ? z : 1) * sizeof(int64_t));
-    if (!S || !s_idx || !blk) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
-    {
-        int64_t t = 0;
-        for (c_i = 0; c_i < z; c_i++) {
-            int64_t lo = Lv[c_i] > W ? Lv[c_i] : W, l;
-            for (l = lo + 1; l <= len[colex[c_i]]; l++) { S[t].c = c_i; S[t].len = l; t++; }
-        }
+    if (!S || !s_idx) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (c_i = 0; c_i < z; c_i++) {
+        int64_t lo = Lv[c_i] > W ? Lv[c_i] : W, l, t = blk[c_i];
+        for (l = lo + 1; l <= len[colex[c_i]]; l++) { S[t].c = c_i; S[t].len = l; t++; }
     }
     /* lexicographic sort of S (K:4408-4552) */
     {
@@ -346,30 +451,65 @@ int gbo_pfp_bwt_ex(const uint8_t *T, int64_t n, int W, int P, int small_alphabet
     }
 
     /* intervals (K:2598-2764), runs (K:3247-3369), mixed blocks
-     * ordered by the next parse suffix (K:3556-4248) */
+     * ordered by the next parse suffix (K:3556-4248).  Every S entry's
+     * interval end first (independent searches), then its block offset,
+     * then the blocks in parallel. */
+    hi_of = (int64_t *)malloc((size_t)(s_n ? s_n : 1) * sizeof(int64_t));
+    boff = (int64_t *)malloc((size_t)(s_n + 1) * sizeof(int64_t));
+    if (!hi_of || !boff) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1024)
+#endif
     for (j = 0; j < s_n; j++) {
         const s_entry *e = &S[s_idx[j]];
-        int64_t lo = e->c, hi = e->c, l = e->len, q;
-        int64_t ia, ib;
-        while (hi + 1 < z && Lv[hi + 1] >= l) hi++;
-        ia = D[colex[lo]] - l; if (ia < 0) ia = n - 1;
-        ib = D[colex[hi]] - l; if (ib < 0) ib = n - 1;
-        if (X[ia] == X[ib]) {
-            for (q = lo; q <= hi; q++) L[out++] = X[ia];
-        } else {
-            mctx mc; mc.next_rank = next_rank; mc.colex = colex;
-            for (q = lo; q <= hi; q++) blk[q - lo] = q;
-            if (msort(blk, hi - lo + 1, cmp_next, &mc)) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
-            for (q = 0; q <= hi - lo; q++) {
-                int64_t ip = D[colex[blk[q]]] - l;
-                if (ip < 0) ip = n - 1;
-                L[out++] = X[ip];
-            }
-            mixed++;
-            mixed_elems += hi - lo + 1;
-        }
+        int64_t hi = e->c;
+        while (hi + 1 < z && Lv[hi + 1] >= e->len) hi++;
+        hi_of[j] = hi;
     }
-    if (out != n) { rc = GBO_INTERNAL_ERROR; goto done; }
+    boff[0] = 0;
+    for (j = 0; j < s_n; j++) {
+        const int64_t b = hi_of[j] - S[s_idx[j]].c + 1;
+        boff[j + 1] = boff[j] + b;
+        if (b > max_blk) max_blk = b;
+    }
+    if (boff[s_n] != n) { rc = GBO_INTERNAL_ERROR; goto done; }
+    {
+        int failed = 0;
+#ifdef _OPENMP
+#pragma omp parallel reduction(+ : mixed, mixed_elems) reduction(| : failed)
+#endif
+        {
+            int64_t *tb = (int64_t *)malloc((size_t)(max_blk ? max_blk : 1) * sizeof(int64_t)), jj;
+            if (!tb) failed = 1;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+            for (jj = 0; jj < s_n; jj++) {
+                const s_entry *e = &S[s_idx[jj]];
+                const int64_t lo = e->c, hi = hi_of[jj], l = e->len;
+                int64_t ia, ib, q, o = boff[jj];
+                if (!tb) continue;
+                ia = D[colex[lo]] - l; if (ia < 0) ia = n - 1;
+                ib = D[colex[hi]] - l; if (ib < 0) ib = n - 1;
+                if (X[ia] == X[ib]) {
+                    for (q = lo; q <= hi; q++) L[o++] = X[ia];
+                } else {
+                    mctx mc; mc.next_rank = next_rank; mc.colex = colex;
+                    for (q = lo; q <= hi; q++) tb[q - lo] = q;
+                    if (msort(tb, hi - lo + 1, cmp_next, &mc)) { failed = 1; continue; }
+                    for (q = 0; q <= hi - lo; q++) {
+                        int64_t ip = D[colex[tb[q]]] - l;
+                        if (ip < 0) ip = n - 1;
+                        L[o++] = X[ip];
+                    }
+                    mixed++;
+                    mixed_elems += hi - lo + 1;
+                }
+            }
+            free(tb);
+        }
+        if (failed) { rc = GBO_NOT_ENOUGH_MEMORY; goto done; }
+    }
 
     if (st) {
         int64_t d = 0, ld = 0;
@@ -386,7 +526,7 @@ int gbo_pfp_bwt_ex(const uint8_t *T, int64_t n, int W, int P, int small_alphabet
 
 done:
     free(X); free(D); free(start); free(len); free(order); free(meta); free(sa);
-    free(next_rank); free(colex); free(Lv); free(S); free(s_idx); free(blk);
+    free(next_rank); free(colex); free(Lv); free(S); free(s_idx); free(blk); free(hi_of); free(boff);
     return rc;
 }
 

@@ -218,7 +218,12 @@ int gbo_unbwt(const uint8_t *L, int64_t n, int64_t pidx, uint8_t *T)
 /* The PFP port runs its stages on one host thread. */
 int gbo_threads_used(void)
 {
+#ifdef _OPENMP
+    extern int omp_get_max_threads(void);
+    return omp_get_max_threads();      /* the PFP port's merge sorts run as OpenMP tasks */
+#else
     return 1;
+#endif
 }
 
 int gbo_max_threads(void)
