@@ -172,6 +172,14 @@ int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, in
 int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n);
 
 /*
+ * libcubwt_bwt_aux's contract (libcubwt.cuh:80-89): the same BWT plus the
+ * auxiliary indexes I[0..(n-1)/r], I[k] = row of the suffix starting at
+ * k*r in libcubwt's numbering (I[0] is the primary index); r a power of two
+ * >= 2.  Host pointers.  Returns GBWT_NO_ERROR.
+ */
+int64_t gbwt_libcubwt_bwt_aux(void *storage, const uint8_t *T, uint8_t *L, int64_t n, int64_t r, uint32_t *I);
+
+/*
  * Inverse BWT on the GPU: L[0..n) as returned by gbwt_pfp_bwt and its
  * primary index (gbwt_stats.primary_index) -> T[0..n).  Host pointers, or
  * device pointers with GBWT_FLAG_DEVICE_POINTERS.  Returns n;

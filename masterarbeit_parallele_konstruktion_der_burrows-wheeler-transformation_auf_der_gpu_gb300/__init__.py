@@ -92,6 +92,7 @@ EXPORTS = (
     "gbwt_libcubwt_bwt", "gbwt_pfp_trigger_scan_noalloc", "gbwt_pfp_bwt_batch", "gbwt_trim_device_storage",
     "gbwt_server_create", "gbwt_server_destroy", "gbwt_submit", "gbwt_poll", "gbwt_wait", "gbwt_server_drain",
     "gbwt_server_peak_admitted", "gbwt_unbwt", "gbwt_libcubwt_unbwt", "gbwt_set_tuning", "gbwt_check_tuning",
+    "gbwt_libcubwt_bwt_aux",
 )
 
 TUNING_KNOBS = ("hash_log2_max", "batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits", "unbwt_rate_log2")
@@ -196,6 +197,8 @@ def _lib() -> ctypes.CDLL:
     L.gbwt_libcubwt_bwt.restype = i64
     L.gbwt_pfp_bwt_batch.argtypes = [vp, u8p, ctypes.c_void_p, i32, u8p, i32, i32, u32]
     L.gbwt_pfp_bwt_batch.restype = i64
+    L.gbwt_libcubwt_bwt_aux.argtypes = [vp, u8p, u8p, i64, i64, ctypes.c_void_p]
+    L.gbwt_libcubwt_bwt_aux.restype = i64
     L.gbwt_set_tuning.argtypes = [vp, ctypes.c_void_p]
     L.gbwt_set_tuning.restype = i64
     L.gbwt_check_tuning.argtypes = [ctypes.c_void_p]
@@ -386,6 +389,16 @@ class Storage:
         _check(_lib().gbwt_libcubwt_unbwt(self.handle, b.ctypes.data, U.ctypes.data, len(b), None, int(primary)),
                "gbwt_libcubwt_unbwt")
         return U[:len(b)]
+
+    def libcubwt_bwt_aux(self, text, r: int) -> tuple[np.ndarray, np.ndarray]:
+        """libcubwt_bwt_aux semantics: (L, I) with I[k] = libcubwt row of the suffix at k*r."""
+        t = _host_u8(text)
+        out = np.empty(max(len(t), 1), dtype=np.uint8)
+        I = np.empty(max((len(t) - 1) // max(int(r), 1) + 1, 1), dtype=np.uint32)
+        self._auto(len(t))
+        _check(_lib().gbwt_libcubwt_bwt_aux(self.handle, t.ctypes.data, out.ctypes.data, len(t), int(r),
+                                            I.ctypes.data), "gbwt_libcubwt_bwt_aux")
+        return out[:len(t)], I
 
     def set_kernel_probe(self, kernel: int) -> None:
         """Time every launch of one kernel family (PROBE_*) from now on."""

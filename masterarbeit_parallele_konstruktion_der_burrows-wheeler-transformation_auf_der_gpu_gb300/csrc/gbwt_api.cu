@@ -404,7 +404,10 @@ __global__ void k_libcubwt_layout(const uint8_t *O, uint8_t *L, uint32_t n, uint
     }
 }
 
-static int64_t libcubwt_bwt(Storage *st, const uint8_t *T, uint8_t *L, int64_t n)
+// libcubwt_bwt (r_log2 < 0) or libcubwt_bwt_aux (sampling rate 2^r_log2,
+// I host array of (n-1) / 2^r_log2 + 1 entries).
+static int64_t libcubwt_bwt(Storage *st, const uint8_t *T, uint8_t *L, int64_t n, int r_log2 = -1,
+                            uint32_t *I = nullptr)
 {
     const uint32_t un = (uint32_t)n;
     uint8_t *dT = slot<uint8_t>(st, S_TEXT, (size_t)n + 16);
@@ -446,9 +449,27 @@ static int64_t libcubwt_bwt(Storage *st, const uint8_t *T, uint8_t *L, int64_t n
     }
     check_cuda(cudaMemcpyAsync(dmaps + 256, hunmap, 256, cudaMemcpyHostToDevice, st->stream));
     uint8_t *dO = slot<uint8_t>(st, S_OUT, (size_t)n + 16);
-    int64_t rc = pipeline(st, dT, dO, n, 5, 16, GBWT_FLAG_DEVICE_POINTERS, UPTO_BWT, nullptr);
-    if (rc < 0) return rc;
-    const uint32_t pidx = (uint32_t)st->stats.primary_index;
+    uint32_t pidx;
+    const size_t ni = r_log2 >= 0 ? (size_t)((n - 1) >> r_log2) + 1 : 0;
+    uint32_t *dI = nullptr;
+    if (r_log2 < 0) {
+        int64_t rc = pipeline(st, dT, dO, n, 5, 16, GBWT_FLAG_DEVICE_POINTERS, UPTO_BWT, nullptr);
+        if (rc < 0) return rc;
+        pidx = (uint32_t)st->stats.primary_index;
+    } else {
+        // every suffix's row is needed at the sampled positions: the batched
+        // path places all of them explicitly (one text)
+        dI = slot<uint32_t>(st, S_GCHAR, ni);
+        const int64_t offs[2] = {0, n};
+        BatchAux aux;
+        aux.r_log2 = r_log2;
+        aux.dI = dI;
+        int64_t rc = run_batch(st, dT, offs, 1, dO, 5, 16, GBWT_FLAG_DEVICE_POINTERS, MAX_N, &aux);
+        if (rc < 0) return rc;
+        check_cuda(cudaMemcpyAsync(I, dI, ni * 4, cudaMemcpyDeviceToHost, st->stream));
+        check_cuda(cudaStreamSynchronize(st->stream));
+        pidx = I[0] - 1u;                       // I[0] is the row of suffix 0, plus one
+    }
     uint8_t *dL = slot<uint8_t>(st, S_LCB, (size_t)n + 16);
     k_libcubwt_layout<<<grid, 256, 0, st->stream>>>(dO, dL, un, pidx, dmaps + 256, T[n - 1]);
     after_launch(st);
@@ -464,6 +485,19 @@ extern "C" int64_t gbwt_libcubwt_bwt(void *storage, const uint8_t *T, uint8_t *L
     Storage *st = (Storage *)storage;
     if (!st || !T || !L || n < 1 || n > MAX_N) return GBWT_BAD_PARAMETER;
     return guarded([&]() { return libcubwt_bwt(st, T, L, n); });
+}
+
+extern "C" int64_t gbwt_libcubwt_bwt_aux(void *storage, const uint8_t *T, uint8_t *L, int64_t n, int64_t r,
+                                         uint32_t *I)
+{
+    Storage *st = (Storage *)storage;
+    if (!st || !T || !L || !I || n < 1 || n > MAX_N || r < 2 || (r & (r - 1)) != 0) return GBWT_BAD_PARAMETER;
+    int r_log2 = 0;
+    while ((1ll << r_log2) < r) r_log2++;
+    return guarded([&]() -> int64_t {
+        const int64_t rc = libcubwt_bwt(st, T, L, n, r_log2, I);
+        return rc < 0 ? rc : GBWT_NO_ERROR;
+    });
 }
 
 extern "C" int64_t gbwt_get_stats(void *storage, gbwt_stats *out)

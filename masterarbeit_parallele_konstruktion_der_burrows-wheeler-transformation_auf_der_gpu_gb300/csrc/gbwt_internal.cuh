@@ -228,7 +228,13 @@ void stage_mark(Storage *st, int idx);
 void pfp_to_libcubwt(Storage *st, const uint8_t *dO, uint32_t n, uint32_t p, uint8_t *dLc);
 void run_unbwt(Storage *st, const uint8_t *dLc, uint32_t n, uint32_t i, uint8_t *dT);
 
+// Sampled suffix array of a one-text batch: aux[p >> r_log2] = row + 1 of
+// the suffix starting at p, for every p that is a multiple of 2^r_log2.
+struct BatchAux {
+    int r_log2 = 0;
+    uint32_t *dI = nullptr;     // device, (n-1) / 2^r_log2 + 1 entries
+};
 int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t k, uint8_t *L, int W, int P,
-                  uint32_t flags, int64_t max_n);
+                  uint32_t flags, int64_t max_n, const BatchAux *aux = nullptr);
 
 }  // namespace gbwt

@@ -132,9 +132,16 @@ struct BatchEmit {
     const uint8_t *X, *lastb;
     uint32_t z;
     int W;
+    const uint32_t *xstart;     // with emx: text starts in X
+    uint32_t *emx;              // optional: the slot's phrase start, text-local
     __device__ __forceinline__ void fill(uint32_t occ, uint32_t s, uint32_t *emq, uint32_t *emt, uint8_t *emp,
                                          uint32_t *ecnt) const
     {
+        if (emx) {
+            const uint32_t t = ptid[occ];
+            const bool first = occ == 0 || X[D[occ - 1]] == 1;
+            emx[s] = first ? 0u : D[occ - 1] - (uint32_t)W + 1u - xstart[t];
+        }
         uint32_t q, prev;
         if (pidpc) {
             const uint32_t v = pidpc[occ];
@@ -174,7 +181,7 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
                                                 const uint32_t *emt, const uint8_t *emp, const uint32_t *pshift,
                                                 const uint32_t *tloc, const uint32_t *grp_of, const uint8_t *dict,
                                                 const uint8_t *enc, int gbb, int bb, E *elem, uint32_t cap,
-                                                uint32_t *flags)
+                                                uint32_t *flags, const uint32_t *emx, uint32_t *epos)
 {
     __shared__ uint32_t s_off[BE_T + 1];
     __shared__ uint32_t s_base[BE_T];
@@ -207,8 +214,12 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
         const uint32_t pos = s_base[lo] + j;
         const uint32_t c = j ? dict[pos - 1] : s_prev[lo];
         const uint32_t dst = o + s_shift[lo];
-        if (dst < cap) elem[dst] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
-        else atomicOr(flags, ERR_INTERNAL);
+        if (dst < cap) {
+            elem[dst] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
+            if (epos) epos[dst] = emx[t0 + lo] + j;        // text-local position of this suffix
+        } else {
+            atomicOr(flags, ERR_INTERNAL);
+        }
     }
 }
 
@@ -216,7 +227,7 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
 // [(b - first) * RS_TILE, +RS_TILE); tout[b] = {output base, real elements}.
 template <typename E>
 __global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, const uint8_t *dec, uint32_t bmask,
-                           uint8_t *out)
+                           uint8_t *out, const uint32_t *epos, int r_log2, uint32_t *aux)
 {
     __shared__ uint8_t s_dec[256];
     s_dec[threadIdx.x] = dec[threadIdx.x];          // blockDim == 256
@@ -227,7 +238,15 @@ __global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, 
     const size_t e0 = (size_t)b * RS_TILE;
     for (uint32_t j = threadIdx.x; j < (uint32_t)RS_TILE; j += 256) {
         const uint32_t p = p0 + j;
-        if (p < to.y) out[to.x + p] = s_dec[(uint32_t)elem[e0 + j] & bmask];
+        if (p < to.y) {
+            out[to.x + p] = s_dec[(uint32_t)elem[e0 + j] & bmask];
+            // sampled suffix array: row (+1, libcubwt's convention) of every
+            // suffix starting at a multiple of 2^r_log2 (one text per call)
+            if (epos) {
+                const uint32_t q = epos[e0 + j];
+                if ((q & ((1u << r_log2) - 1u)) == 0) aux[q >> r_log2] = p + 1u;
+            }
+        }
     }
 }
 
@@ -324,15 +343,18 @@ template <typename E>
 static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dmeta, uint32_t S,
                          const uint32_t *eoff, const uint32_t *emq, const uint32_t *emt, const uint8_t *emp,
                          const uint32_t *grp_of, const uint8_t *dict, const uint8_t *codes, int gb, int bb, int tlb,
-                         uint8_t *dOut)
+                         uint8_t *dOut, const uint32_t *emx, const BatchAux *aux)
 {
     const uint32_t M = bl.tiles * (uint32_t)RS_TILE;
     E *elem = slot<E>(st, S_ELEM0, M);
     E *elem_alt = slot<E>(st, S_ELEM1, M);
+    uint32_t *pos = aux ? slot<uint32_t>(st, S_VAL0, M) : nullptr;
+    uint32_t *pos_alt = aux ? slot<uint32_t>(st, S_VAL1, M) : nullptr;
     check_cuda(cudaMemsetAsync(elem, 0xFF, (size_t)M * sizeof(E), st->stream));    // padding keys
+    if (aux) check_cuda(cudaMemsetAsync(pos, 0xFF, (size_t)M * 4, st->stream));
     k_bemit<E><<<grid_for(S, BE_T), BE_T, 0, st->stream>>>(S, eoff, emq, emt, emp, dmeta + bl.o_pshift,
                                                            dmeta + bl.o_tloc, grp_of, dict, codes, gb + bb, bb, elem,
-                                                           M, st->d_flags);
+                                                           M, st->d_flags, emx, pos);
     after_launch(st);
     const uint2 *tseg = (const uint2 *)(dmeta + bl.o_tseg);
     // sort by (text, group) only: the byte rides along, and elements of one
@@ -343,16 +365,18 @@ static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dme
     uint32_t *nv = nullptr, *nv2 = nullptr;
     const int want = st->tuning.batch_radix_bits;
     const bool nine = want ? want == 9 : (sb + 8) / 9 < (sb + 7) / 8;
-    if (nine) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    if (aux) radix_sort<E, true, 8>(st, elem, elem_alt, pos, pos_alt, M, bb, bb + sb, tseg);
+    else if (nine) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
     stage_mark(st, 5);
     k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,
-                                                    (1u << bb) - 1u, dOut);
+                                                    (1u << bb) - 1u, dOut, pos, aux ? aux->r_log2 : 0,
+                                                    aux ? aux->dI : nullptr);
     after_launch(st);
 }
 
 int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t k, uint8_t *L, int W, int P,
-                  uint32_t flags, int64_t max_n)
+                  uint32_t flags, int64_t max_n, const BatchAux *aux)
 {
     if (!offsets || k < 0 || W < 1 || W > 64 || P < 1 || P > 65535) return GBWT_BAD_PARAMETER;
     if (offsets[0] != 0) return GBWT_BAD_PARAMETER;
@@ -467,7 +491,9 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     uint32_t *emt = slot<uint32_t>(st, S_TMP1, S);
     uint8_t *emp = slot<uint8_t>(st, S_TMP2, S);
     uint32_t *ecnt = slot<uint32_t>(st, S_GCOUNT, (size_t)S + 1);
-    BatchEmit e{psa_tm, ph.pid, ph.pidpc, ph.D, ptid, zend, ph.dlen, ph.doff, X, lastb, z, W};
+    uint32_t *emx = aux ? slot<uint32_t>(st, S_TILEG, S) : nullptr;
+    if (aux && kk != 1) throw Error{GBWT_BAD_PARAMETER};
+    BatchEmit e{psa_tm, ph.pid, ph.pidpc, ph.D, ptid, zend, ph.dlen, ph.doff, X, lastb, z, W, xstart, emx};
     k_bemit_prep<<<grid_for(z, 256), 256, 0, st->stream>>>(e, emq, emt, emp, ecnt);
     after_launch(st);
     device_scan<uint32_t, OpAdd>(st, S, LoadArr<uint32_t>{ecnt}, StoreArr<uint32_t>{ecnt}, false, ecnt + S);
@@ -476,9 +502,11 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     if ((uint32_t)st->h_scalars[0] != (uint32_t)total) throw Error{GBWT_INTERNAL_ERROR};
     st->stats.mixed_elems = (int64_t)bl.tiles * RS_TILE;     // padded element count
     if (tlb + gb + bb <= 32)
-        batch_output<uint32_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut);
+        batch_output<uint32_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut, emx,
+                               aux);
     else
-        batch_output<uint64_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut);
+        batch_output<uint64_t>(st, bl, meta, S, ecnt, emq, emt, emp, grp_of, ph.dict, codes, gb, bb, tlb, dOut, emx,
+                               aux);
     stage_mark(st, 6);
     if (!devptr) check_cuda(cudaMemcpyAsync(L, dOut, (size_t)total, cudaMemcpyDeviceToHost, st->stream));
     check_cuda(cudaMemcpyAsync(st->h_scalars + 8, st->d_flags, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost,

@@ -67,3 +67,23 @@ def test_libcubwt_too_many_symbols(storage, pkg):
     with pytest.raises(pkg.GbwtError) as e:
         storage.libcubwt_bwt(t)
     assert e.value.code == pkg.UNSUPPORTED_INPUT
+
+
+@pytest.mark.parametrize("r", [2, 4, 32])
+def test_libcubwt_aux_indexes(storage, orc, wl, r):
+    rng = np.random.default_rng(r)
+    cases = [rng.integers(0, 256, size=5000).astype(np.uint8), np.array([7], np.uint8),
+             rng.integers(10, 13, size=333).astype(np.uint8), wl.dna_copies(base_len=8192, copies=12, seed=r)]
+    for t in cases:
+        t = t.copy()
+        if len(np.unique(t)) > 253:
+            t[t > 252] = 252
+        L, I = storage.libcubwt_bwt_aux(t, r)
+        L0, idx = storage.libcubwt_bwt(t)
+        assert np.array_equal(L, L0)
+        sa = orc.suffix_array(t)
+        isa = np.empty(len(t), np.int64)
+        isa[sa] = np.arange(len(t))
+        want = isa[::r] + 1
+        assert np.array_equal(I.astype(np.int64), want), (len(t), r)
+        assert I[0] == idx
