@@ -214,7 +214,10 @@ typedef struct gbwt_tuning {
                                    many eighths of the elements (0..64; default 1)                   */
     int32_t batch_radix_bits;   /* batch output sort digit width: 8, 9, or 0 = fewest passes         */
     int32_t unbwt_rate_log2;    /* inverse BWT: one ruler per 2^k rows (2..12; default 7)            */
-    int32_t reserved[3];
+    int32_t dict_key_bits;      /* dictionary sort, first key: at most this many bits of recoded
+                                   symbols (8..64; default 64: as many symbols as fit)             */
+    int32_t parse_key_phrases;  /* parse suffix array, first key: 1 or 2 phrase ranks (default 2)  */
+    int32_t reserved[1];
 } gbwt_tuning;
 
 /* Sets (t != NULL) or resets (t == NULL) the storage's tuning. */

@@ -10,9 +10,9 @@ density), never a result; tests check that.
   python -m <package>.autotune                      # classes 16, 128, 512 MiB
   python -m <package>.autotune --classes 64 --repeats 5 --out /tmp/t.json
 
-Each class is measured on the batched workload's text mix scaled to the
-class's total size (batched knobs and the hash table) and on one repetitive
-DNA text of that size (inverse-BWT rulers).
+Each class is measured on one repetitive DNA text of that size (hash table,
+first sort keys, inverse-BWT rulers) and on the batched workload's text mix
+scaled to the class's total size (batch knobs).
 """
 from __future__ import annotations
 
@@ -29,14 +29,17 @@ PKG = os.path.basename(os.path.dirname(os.path.abspath(__file__)))
 # candidate values per knob; 0 in a result means the library default
 CANDIDATES = {
     "hash_log2_max": (20, 22, 24),
+    "dict_key_bits": (64, 48, 40, 32),
+    "parse_key_phrases": (1, 2),
     "batch_seg_tiles": (4, 8, 16, 32),
     "batch_pad_eighths": (1, 2, 4),
     "batch_radix_bits": (8, 9),
     "unbwt_rate_log2": (6, 7, 8),
 }
-BATCH_KNOBS = ("hash_log2_max", "batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits")
-START = {"hash_log2_max": 22, "batch_seg_tiles": 8, "batch_pad_eighths": 1, "batch_radix_bits": 0,
-         "unbwt_rate_log2": 7}
+TEXT_KNOBS = ("hash_log2_max", "dict_key_bits", "parse_key_phrases")
+BATCH_KNOBS = ("batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits")
+START = {"hash_log2_max": 22, "dict_key_bits": 64, "parse_key_phrases": 2, "batch_seg_tiles": 8,
+         "batch_pad_eighths": 1, "batch_radix_bits": 0, "unbwt_rate_log2": 7}
 
 
 def coordinate_descent(measure, knobs, start: dict, candidates: dict = CANDIDATES, sweeps: int = 2):
@@ -89,27 +92,35 @@ def _median_ms(fn, repeats):
 def tune_class(pkg, wl, mib: int, repeats: int, log) -> dict:
     import torch
 
-    scale = mib / 512.0
-    count = max(8, int(round(4096 * scale)))
+    # one repetitive DNA text of the class size: hash table and first keys
+    text = wl.dna_copies(base_len=max(4096, (mib << 20) // 64), copies=64, seed=50 + mib, indel_rate=1e-4)
+    d_text = torch.from_numpy(text).cuda()
+    d_bwt = torch.empty_like(d_text)
+    st = pkg.Storage(len(text), tuning=None)
+    st.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    def measure_text(cfg):
+        st.set_tuning(cfg)
+        return _median_ms(lambda: st.pfp_bwt_device(d_text.data_ptr(), d_bwt.data_ptr(), len(text)), repeats)
+
+    best, t_best, runs = coordinate_descent(measure_text, TEXT_KNOBS, START)
+    log(f"  {mib} MiB text: {t_best:.2f} ms after {runs} configurations: {best}")
+    # the batched workload's text mix scaled to the class size: batch knobs
+    count = max(8, int(round(4096 * mib / 512.0)))
     concat, offsets = wl.batch_texts(count, scale=1.0, seed=40 + mib)
     dT = torch.from_numpy(concat).cuda()
     dL = torch.empty_like(dT)
-    st = pkg.Storage(len(concat), tuning=None)
-    st.set_stream(torch.cuda.current_stream().cuda_stream)
 
     def measure_batch(cfg):
         st.set_tuning(cfg)
         return _median_ms(lambda: st.pfp_bwt_batch_device(dT.data_ptr(), offsets, dL.data_ptr()), repeats)
 
-    best, t_best, runs = coordinate_descent(measure_batch, BATCH_KNOBS, START)
+    best, t_best, runs = coordinate_descent(measure_batch, BATCH_KNOBS, best)
     log(f"  {mib} MiB batch ({count} texts): {t_best:.2f} ms after {runs} configurations: {best}")
     del dT, dL
-    # inverse BWT rulers on one repetitive text of the class size
-    text = wl.dna_copies(base_len=max(4096, (mib << 20) // 64), copies=64, seed=50 + mib)
-    d_text = torch.from_numpy(text).cuda()
-    d_bwt = torch.empty_like(d_text)
+    # inverse BWT rulers on the text
     d_back = torch.empty_like(d_text)
-    st.set_tuning(None)
+    st.set_tuning(best)
     st.pfp_bwt_device(d_text.data_ptr(), d_bwt.data_ptr(), len(text))
     torch.cuda.synchronize()
     primary = st.stats()["primary_index"]
@@ -118,12 +129,11 @@ def tune_class(pkg, wl, mib: int, repeats: int, log) -> dict:
         st.set_tuning(cfg)
         return _median_ms(lambda: st.unbwt_device(d_bwt.data_ptr(), d_back.data_ptr(), len(text), primary), repeats)
 
-    ub, t_ub, runs_ub = coordinate_descent(measure_unbwt, ("unbwt_rate_log2",), {"unbwt_rate_log2": 7})
+    best, t_ub, runs_ub = coordinate_descent(measure_unbwt, ("unbwt_rate_log2",), best)
     if not torch.equal(d_back, d_text):
         raise SystemExit("autotune: inverse BWT does not give the text back")
-    log(f"  {mib} MiB inverse BWT: {t_ub:.2f} ms, {ub}")
+    log(f"  {mib} MiB inverse BWT: {t_ub:.2f} ms, rate 2^{best['unbwt_rate_log2']}")
     st.close()
-    best.update(ub)
     return {k: int(v) for k, v in best.items()}
 
 

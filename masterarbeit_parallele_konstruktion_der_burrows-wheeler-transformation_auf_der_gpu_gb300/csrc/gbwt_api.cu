@@ -518,7 +518,9 @@ extern "C" int64_t gbwt_check_tuning(const gbwt_tuning *t)
                     (t->batch_seg_tiles >= 0 && t->batch_seg_tiles <= 1024) &&
                     (t->batch_pad_eighths >= 0 && t->batch_pad_eighths <= 64) &&
                     (t->batch_radix_bits == 0 || t->batch_radix_bits == 8 || t->batch_radix_bits == 9) &&
-                    (t->unbwt_rate_log2 == 0 || (t->unbwt_rate_log2 >= 2 && t->unbwt_rate_log2 <= 12));
+                    (t->unbwt_rate_log2 == 0 || (t->unbwt_rate_log2 >= 2 && t->unbwt_rate_log2 <= 12)) &&
+                    (t->dict_key_bits == 0 || (t->dict_key_bits >= 8 && t->dict_key_bits <= 64)) &&
+                    (t->parse_key_phrases >= 0 && t->parse_key_phrases <= 2);
     return ok ? GBWT_NO_ERROR : GBWT_BAD_PARAMETER;
 }
 

@@ -142,6 +142,11 @@ inline int tune_hash_log2(const Storage *st) { return st->tuning.hash_log2_max ?
 inline int tune_seg_tiles(const Storage *st) { return st->tuning.batch_seg_tiles ? st->tuning.batch_seg_tiles : 8; }
 inline int tune_pad_eighths(const Storage *st) { return st->tuning.batch_pad_eighths ? st->tuning.batch_pad_eighths : 1; }
 inline int tune_unbwt_rate_log2(const Storage *st) { return st->tuning.unbwt_rate_log2 ? st->tuning.unbwt_rate_log2 : 7; }
+inline int tune_dict_key_bits(const Storage *st) { return st->tuning.dict_key_bits ? st->tuning.dict_key_bits : 64; }
+inline int tune_parse_key_phrases(const Storage *st)
+{
+    return st->tuning.parse_key_phrases ? st->tuning.parse_key_phrases : 2;
+}
 
 inline int bits_for(uint64_t v)   // bits needed to represent values in [0, v]
 {

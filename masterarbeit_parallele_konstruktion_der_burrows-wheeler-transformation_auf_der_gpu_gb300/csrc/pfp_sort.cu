@@ -775,7 +775,10 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
         hcode[c] = p ? (uint8_t)(++sigma) : 0;
     }
     const int bps = bits_for(sigma);                           // codes 0..sigma
-    const int h0 = 63 / bps;
+    // as many symbols as fit the first key's bit budget (radix passes over
+    // the dictionary vs later doubling rounds: a tuning knob)
+    const int key_bits = tune_dict_key_bits(st);
+    const int h0 = (key_bits - 1) / bps > 0 ? (key_bits - 1) / bps : 1;
     uint8_t *dcode = slot<uint8_t>(st, S_TMP1, 256);
     check_cuda(cudaMemcpyAsync(dcode, hcode, 256, cudaMemcpyHostToDevice, st->stream));
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, N);
@@ -789,11 +792,15 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
                                  StoreLexRank{dord.sa, ph.dphr, dord.lexrank}, false, (uint32_t *)nullptr);
 }
 
-__global__ void k_parse_keys(const uint32_t *pid, const uint32_t *lexrank, uint32_t z, int lb, uint64_t *keys)
+// First parse key: one phrase rank (two == false), or two (the second 0
+// past the parse end).
+__global__ void k_parse_keys(const uint32_t *pid, const uint32_t *lexrank, uint32_t z, int lb, bool two,
+                             uint64_t *keys)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= z) return;
     uint64_t a = lexrank[pid[i]];
+    if (!two) { keys[i] = a; return; }
     uint64_t b = i + 1 < z ? (uint64_t)lexrank[pid[i + 1]] + 1u : 0u;
     keys[i] = (a << lb) | b;
 }
@@ -803,20 +810,23 @@ void run_parse_sa(Storage *st, Phrases &ph, DictOrder &dord, ParseOrder &pord)
     const uint32_t z = ph.z;
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
     const int lb = bits_for(ph.d);       // lexrank+1 <= d
-    k_parse_keys<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, z, lb, keys);
+    const bool two = tune_parse_key_phrases(st) == 2;
+    k_parse_keys<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, z, lb, two, keys);
     after_launch(st);
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
-    pord.rounds = prefix_doubling(st, z, lb + bits_for(ph.d - 1), 2u, ParseRem{z}, pord.isa, pord.sa);
+    pord.rounds = prefix_doubling(st, z, two ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), two ? 2u : 1u,
+                                  ParseRem{z}, pord.isa, pord.sa);
 }
 
 // Batch: the second symbol of a key is 0 when phrase i ends its text.
 __global__ void k_parse_keys_batch(const uint32_t *pid, const uint32_t *lexrank, const uint32_t *ptid, uint32_t z,
-                                   int lb, uint64_t *keys)
+                                   int lb, bool two, uint64_t *keys)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= z) return;
     uint64_t a = lexrank[pid[i]];
+    if (!two) { keys[i] = a; return; }
     uint64_t b = (i + 1 < z && ptid[i + 1] == ptid[i]) ? (uint64_t)lexrank[pid[i + 1]] + 1u : 0u;
     keys[i] = (a << lb) | b;
 }
@@ -829,11 +839,13 @@ void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchTe
     const uint32_t z = ph.z;
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
     const int lb = bits_for(ph.d);
-    k_parse_keys_batch<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bt.ptid, z, lb, keys);
+    const bool two = tune_parse_key_phrases(st) == 2;
+    k_parse_keys_batch<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bt.ptid, z, lb, two, keys);
     after_launch(st);
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
-    pord.rounds = prefix_doubling(st, z, lb + bits_for(ph.d - 1), 2u, BatchParseRem{bt.ptid, bt.zend}, pord.isa,
+    pord.rounds = prefix_doubling(st, z, two ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), two ? 2u : 1u,
+                                  BatchParseRem{bt.ptid, bt.zend}, pord.isa,
                                   pord.sa);
 }
 

@@ -40,7 +40,8 @@ def test_tuning_for_size_classes(pkg):
 def test_library_validates_knobs(pkg):
     assert pkg.check_tuning({})
     assert pkg.check_tuning({"hash_log2_max": 24, "batch_radix_bits": 9, "unbwt_rate_log2": 6})
-    for bad in ({"hash_log2_max": 8}, {"batch_radix_bits": 10}, {"unbwt_rate_log2": 20}, {"batch_seg_tiles": -1}):
+    for bad in ({"hash_log2_max": 8}, {"batch_radix_bits": 10}, {"unbwt_rate_log2": 20}, {"batch_seg_tiles": -1},
+                {"dict_key_bits": 4}, {"parse_key_phrases": 3}):
         assert not pkg.check_tuning(bad), bad
     with pytest.raises(ValueError):
         pkg.Tuning.from_dict({"no_such_knob": 1})

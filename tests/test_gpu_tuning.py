@@ -7,7 +7,8 @@ pytestmark = pytest.mark.gpu
 
 CONFIGS = [None, {"hash_log2_max": 16}, {"hash_log2_max": 24, "batch_radix_bits": 8},
            {"batch_seg_tiles": 1, "batch_pad_eighths": 64, "batch_radix_bits": 9},
-           {"batch_seg_tiles": 64, "batch_pad_eighths": 0}, {"unbwt_rate_log2": 2}, {"unbwt_rate_log2": 12}]
+           {"batch_seg_tiles": 64, "batch_pad_eighths": 0}, {"unbwt_rate_log2": 2}, {"unbwt_rate_log2": 12},
+           {"dict_key_bits": 8, "parse_key_phrases": 1}, {"dict_key_bits": 33}]
 
 
 def test_batch_and_single_results_do_not_depend_on_tuning(pkg, wl):
