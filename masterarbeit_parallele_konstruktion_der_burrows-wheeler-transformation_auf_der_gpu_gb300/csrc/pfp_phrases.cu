@@ -138,7 +138,20 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     a.slot_of[k] = pos;
 }
 
+// 8 text bytes starting at T + p (any alignment): two aligned 8-byte loads
+// and a shift.  The caller keeps T + p + 16 inside the buffer.
+__device__ __forceinline__ uint64_t load8_any(const uint8_t *T, uint32_t p)
+{
+    const uintptr_t a = (uintptr_t)(T + p);
+    const uint64_t *w = (const uint64_t *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7u) * 8u;
+    const uint64_t lo = __ldg(w), hi = __ldg(w + 1);
+    return sh ? (lo >> sh) | (hi << (64u - sh)) : lo;
+}
+
 // Compares each occurrence with its representative; marks representatives.
+// Inside the text 8 bytes at a time; the tail and the sentinel run after
+// the text byte by byte.
 __global__ void k_phrase_verify(const uint8_t *T, uint32_t n, const uint32_t *D, uint32_t z, int W,
                                 const uint32_t *tvals, const uint32_t *slot_of, uint32_t *isrep, uint32_t *flags,
                                 const uint8_t *xsep)
@@ -154,7 +167,16 @@ __global__ void k_phrase_verify(const uint8_t *T, uint32_t n, const uint32_t *D,
     phrase_span(D, rep, W, xsep, s2, e2);
     if (e1 - s1 != e2 - s2) { atomicOr(flags, ERR_COLLISION); return; }
     const uint32_t len = e1 - s1 + 1u;
-    for (uint32_t i = 0; i < len; i++) {
+    const uint32_t hi_start = s1 > s2 ? s1 : s2;
+    // words only where both 16-byte load windows stay inside the n text bytes
+    // (an 8-byte aligned text: the aligned loads never start before it)
+    const uint32_t inside = (((uintptr_t)T & 7u) == 0 && n > hi_start + 16u) ? n - hi_start - 16u : 0u;
+    const uint32_t wlen = (len < inside ? len : inside) & ~7u;
+    uint32_t i = 0;
+    for (; i < wlen; i += 8) {
+        if (load8_any(T, s1 + i) != load8_any(T, s2 + i)) { atomicOr(flags, ERR_COLLISION); return; }
+    }
+    for (; i < len; i++) {
         if (text_at(T, n, s1 + i) != text_at(T, n, s2 + i)) { atomicOr(flags, ERR_COLLISION); return; }
     }
 }
