@@ -217,7 +217,7 @@ typedef struct gbwt_tuning {
     int32_t dict_key_bits;      /* dictionary sort, first key: at most this many bits of recoded
                                    symbols (8..64; default 64: as many symbols as fit)             */
     int32_t parse_key_phrases;  /* parse suffix array, first key: 1 or 2 phrase ranks (default 2)  */
-    int32_t reserved[1];
+    int32_t mixed_radix_bits;   /* mixed-block element sort digit width: 8 or 10 (default 8)       */
 } gbwt_tuning;
 
 /* Sets (t != NULL) or resets (t == NULL) the storage's tuning. */

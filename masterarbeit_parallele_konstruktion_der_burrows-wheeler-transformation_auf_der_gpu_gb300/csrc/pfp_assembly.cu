@@ -382,8 +382,10 @@ static void mixed_blocks(Storage *st, const uint8_t *dT, uint32_t n, int W, Phra
     k_emit<E><<<grid_for(z, EM_T), EM_T, 0, st->stream>>>(z, ecnt, emq, emp, moff, mb, mc, elem, M, st->d_flags);
     after_launch(st);
     uint32_t *nv = nullptr, *nv2 = nullptr;
-    // sort by block id (8-bit digits: measured faster per byte than 10-bit ones)
-    radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, 8, 8 + bits_for(B - 1));
+    // sort by block id; 8-bit digits unless the tuning asks for 10 (fewer
+    // passes, larger tile histograms)
+    if (st->tuning.mixed_radix_bits == 10) radix_sort<E, false, 10>(st, elem, elem_alt, nv, nv2, M, 8, 8 + bits_for(B - 1));
+    else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, 8, 8 + bits_for(B - 1));
     probe_begin(st, GBWT_PROBE_MIXED_SCATTER);
     k_mixed_scatter<E><<<grid_for((M + 3) / 4, 256), 256, 0, st->stream>>>(elem, M, delta, B, dOut, n, st->d_flags);
     probe_end(st, GBWT_PROBE_MIXED_SCATTER, (uint64_t)M * (sizeof(E) + 1));

@@ -207,33 +207,27 @@ struct StoreDense {
 };
 
 // pid per occurrence; occurrence counts and the min/max preceding byte of
-// every distinct phrase (warp-aggregated over equal ids).
+// every distinct phrase.
 __global__ void k_phrase_finalize(const uint8_t *T, uint32_t n, const uint32_t *D, uint32_t z, int W,
                                   const uint32_t *slot_of, const uint32_t *tdense, uint32_t *pid, uint32_t *pidpc,
                                   uint32_t *occ, uint32_t *pcmin, uint32_t *pcmax, const uint8_t *xsep,
                                   const uint32_t *ptid, const uint8_t *lastb)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = k < z;
-    uint32_t id = 0xFFFFFFFFu, c = 0;
-    if (valid) {
-        id = tdense[slot_of[k]];
-        pid[k] = id;
-        uint32_t s, e;
-        phrase_span(D, k, W, xsep, s, e);
-        // the first phrase of a text is preceded by the text's last byte
-        if (xsep && (k == 0 || xsep[D[k - 1]] == 1)) c = lastb[ptid[k]];
-        else c = preceding_byte(T, n, s);
-        if (pidpc) pidpc[k] = (id << 8) | c;     // only when ids fit 24 bits
-    }
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, id);
-    const uint32_t cmin = __reduce_min_sync(peers, c);
-    const uint32_t cmax = __reduce_max_sync(peers, c);
-    if (valid && (threadIdx.x & 31u) == (unsigned)(__ffs(peers) - 1)) {
-        atomicAdd(occ + id, (uint32_t)__popc(peers));
-        atomicMin(pcmin + id, cmin);
-        atomicMax(pcmax + id, cmax);
-    }
+    if (k >= z) return;
+    const uint32_t id = tdense[slot_of[k]];
+    pid[k] = id;
+    uint32_t s, e, c;
+    phrase_span(D, k, W, xsep, s, e);
+    // the first phrase of a text is preceded by the text's last byte
+    if (xsep && (k == 0 || xsep[D[k - 1]] == 1)) c = lastb[ptid[k]];
+    else c = preceding_byte(T, n, s);
+    if (pidpc) pidpc[k] = (id << 8) | c;     // only when ids fit 24 bits
+    // one atomic each per occurrence: neighbouring occurrences rarely share a
+    // phrase, so warp aggregation (a match per warp) costs more than it saves
+    atomicAdd(occ + id, 1u);
+    atomicMin(pcmin + id, c);
+    atomicMax(pcmax + id, c);
 }
 
 struct LoadLen64 {
