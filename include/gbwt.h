@@ -218,6 +218,9 @@ typedef struct gbwt_tuning {
                                    symbols (8..64; default 64: as many symbols as fit)             */
     int32_t parse_key_phrases;  /* parse suffix array, first key: 1 or 2 phrase ranks (default 2)  */
     int32_t mixed_radix_bits;   /* mixed-block element sort digit width: 8 or 10 (default 8)       */
+    int32_t batch_ballot;       /* batch output sort ranking: every k-th item by ballots (2 or 3),
+                                   1 = match only (default 3)                                       */
+    int32_t reserved[3];
 } gbwt_tuning;
 
 /* Sets (t != NULL) or resets (t == NULL) the storage's tuning. */

@@ -96,12 +96,12 @@ EXPORTS = (
 )
 
 TUNING_KNOBS = ("hash_log2_max", "batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits", "unbwt_rate_log2",
-                "dict_key_bits", "parse_key_phrases", "mixed_radix_bits")
+                "dict_key_bits", "parse_key_phrases", "mixed_radix_bits", "batch_ballot")
 
 
 class Tuning(ctypes.Structure):
     """gbwt_tuning (include/gbwt.h): scheduling knobs, 0 = default."""
-    _fields_ = [(k, ctypes.c_int32) for k in TUNING_KNOBS]
+    _fields_ = [(k, ctypes.c_int32) for k in TUNING_KNOBS] + [("reserved", ctypes.c_int32 * 3)]
 
     @classmethod
     def from_dict(cls, d: dict | None) -> "Tuning":

@@ -35,12 +35,13 @@ CANDIDATES = {
     "batch_seg_tiles": (4, 8, 16, 32),
     "batch_pad_eighths": (1, 2, 4),
     "batch_radix_bits": (8, 9),
+    "batch_ballot": (1, 2, 3),
     "unbwt_rate_log2": (6, 7, 8),
 }
 TEXT_KNOBS = ("hash_log2_max", "dict_key_bits", "parse_key_phrases", "mixed_radix_bits")
-BATCH_KNOBS = ("batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits")
+BATCH_KNOBS = ("batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits", "batch_ballot")
 START = {"hash_log2_max": 22, "dict_key_bits": 64, "parse_key_phrases": 2, "mixed_radix_bits": 8, "batch_seg_tiles": 8,
-         "batch_pad_eighths": 1, "batch_radix_bits": 0, "unbwt_rate_log2": 7}
+         "batch_pad_eighths": 1, "batch_radix_bits": 0, "batch_ballot": 3, "unbwt_rate_log2": 7}
 
 
 def coordinate_descent(measure, knobs, start: dict, candidates: dict = CANDIDATES, sweeps: int = 2):

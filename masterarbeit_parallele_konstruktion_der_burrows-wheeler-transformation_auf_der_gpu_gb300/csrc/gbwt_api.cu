@@ -521,7 +521,8 @@ extern "C" int64_t gbwt_check_tuning(const gbwt_tuning *t)
                     (t->unbwt_rate_log2 == 0 || (t->unbwt_rate_log2 >= 2 && t->unbwt_rate_log2 <= 12)) &&
                     (t->dict_key_bits == 0 || (t->dict_key_bits >= 8 && t->dict_key_bits <= 64)) &&
                     (t->parse_key_phrases >= 0 && t->parse_key_phrases <= 2) &&
-                    (t->mixed_radix_bits == 0 || t->mixed_radix_bits == 8 || t->mixed_radix_bits == 10);
+                    (t->mixed_radix_bits == 0 || t->mixed_radix_bits == 8 || t->mixed_radix_bits == 10) &&
+                    (t->batch_ballot >= 0 && t->batch_ballot <= 3);
     return ok ? GBWT_NO_ERROR : GBWT_BAD_PARAMETER;
 }
 

@@ -365,9 +365,19 @@ static void batch_output(Storage *st, const BatchLayout &bl, const uint32_t *dme
     uint32_t *nv = nullptr, *nv2 = nullptr;
     const int want = st->tuning.batch_radix_bits;
     const bool nine = want ? want == 9 : (sb + 8) / 9 < (sb + 7) / 8;
+    // keys-only passes rank every k-th item with ballots (uniform group
+    // digits make the match-only ranking pipe-bound; tuning knob)
+    const int bal = st->tuning.batch_ballot ? st->tuning.batch_ballot : 3;
     if (aux) radix_sort<E, true, 8>(st, elem, elem_alt, pos, pos_alt, M, bb, bb + sb, tseg);
-    else if (nine) radix_sort<E, false, 9>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
-    else radix_sort<E, false, 8>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    else if (nine) {
+        if (bal == 2) radix_sort<E, false, 9, 2>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+        else if (bal == 3) radix_sort<E, false, 9, 3>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+        else radix_sort<E, false, 9, 0>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    } else {
+        if (bal == 2) radix_sort<E, false, 8, 2>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+        else if (bal == 3) radix_sort<E, false, 8, 3>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+        else radix_sort<E, false, 8, 0>(st, elem, elem_alt, nv, nv2, M, bb, bb + sb, tseg);
+    }
     stage_mark(st, 5);
     k_bextract<E><<<bl.tiles, 256, 0, st->stream>>>(elem, tseg, (const uint2 *)(dmeta + bl.o_tout), codes + 256,
                                                     (1u << bb) - 1u, dOut, pos, aux ? aux->r_log2 : 0,

@@ -191,6 +191,31 @@ __device__ __forceinline__ uint32_t rs_digit(K k, int shift, uint32_t mask)
     return (uint32_t)(k >> shift) & mask;
 }
 
+// Ranking can split its items between two warp multisplits so that both
+// issue pipes work: __match_any_sync (one instruction, limited by its pipe)
+// and one ballot per digit bit (ALU work); every BALLOT-th item uses ballots
+// (template argument, 0 = never).  Measured on GB300 for the batched output
+// sort (u32 keys, uniform 8-bit digits): 727 us per pass with match only,
+// 595 us with BALLOT = 3, 580 us with BALLOT = 2.  The match instruction's
+// cost grows with the number of distinct digits in a warp, so sorts whose
+// warps see few distinct digits keep match only.
+
+// Lanes of the warp holding the same digit d (< 2^BITS, or 0xFFFFFFFF for
+// no key: those lanes form their own class).
+template <int BITS>
+__device__ __forceinline__ unsigned rs_peers_ballot(uint32_t d)
+{
+    const bool valid = d != 0xFFFFFFFFu;
+    const unsigned vm = __ballot_sync(0xFFFFFFFFu, valid);
+    unsigned m = valid ? vm : ~vm;
+#pragma unroll
+    for (int b = 0; b < BITS; b++) {
+        const unsigned v = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+        m &= ((d >> b) & 1u) ? v : ~v;
+    }
+    return m;
+}
+
 
 // Histogram slot of digit d for tile b.  Unsegmented: digit-major over all
 // tiles.  Segmented (tseg[b] = {first tile, tiles} of b's segment, every
@@ -252,7 +277,7 @@ constexpr size_t rs_smem_bytes()
            (size_t)(1 << BITS) * 4 * 2 + 32 * 4;
 }
 
-template <typename K, bool HAS_VAL, int BITS>
+template <typename K, bool HAS_VAL, int BITS, int BALLOT>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict__ kin, K *__restrict__ kout,
                                                              const uint32_t *__restrict__ vin,
                                                              uint32_t *__restrict__ vout, uint32_t n, int shift,
@@ -293,7 +318,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
         // the lowest lane of each digit class reads and advances the warp's
         // counter; the others take the old value from it
         const uint32_t d = dg[i];
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned peers = (BALLOT > 0 && i % (BALLOT > 0 ? BALLOT : 1) == (BALLOT > 0 ? BALLOT - 1 : 0))
+                                   ? rs_peers_ballot<BITS>(d)
+                                   : __match_any_sync(0xFFFFFFFFu, d);
         const unsigned leader = (unsigned)(__ffs(peers) - 1);
         uint32_t prior = 0;
         if (lane == leader && d != 0xFFFFFFFFu) {
@@ -357,7 +384,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *__restrict
 // return `keys` and `vals` point at the sorted data (the *_alt buffers hold
 // garbage).  With `tseg` (see rs_hist_index; n a multiple of RS_TILE) every
 // segment is sorted on its own.
-template <typename K, bool HAS_VAL, int BITS = 8>
+template <typename K, bool HAS_VAL, int BITS = 8, int BALLOT = 0>
 void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *&vals_alt, uint32_t n,
                 int begin_bit, int end_bit, const uint2 *tseg = nullptr)
 {
@@ -366,7 +393,7 @@ void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *
     static bool attr_set = false;
     constexpr size_t smem = rs_smem_bytes<K, HAS_VAL, BITS>();
     if (!attr_set) {
-        check_cuda(cudaFuncSetAttribute(k_rs_downsweep<K, HAS_VAL, BITS>,
+        check_cuda(cudaFuncSetAttribute(k_rs_downsweep<K, HAS_VAL, BITS, BALLOT>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
@@ -380,7 +407,7 @@ void radix_sort(Storage *st, K *&keys, K *&keys_alt, uint32_t *&vals, uint32_t *
         after_launch(st);
         scan_array_excl<uint32_t, OpAdd>(st, hist, D * num_tiles, 0);
         probe_begin(st, GBWT_PROBE_RADIX_SCATTER);
-        k_rs_downsweep<K, HAS_VAL, BITS><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt,
+        k_rs_downsweep<K, HAS_VAL, BITS, BALLOT><<<num_tiles, RS_THREADS, smem, st->stream>>>(keys, keys_alt, vals, vals_alt,
                                                                                       n, shift, mask, hist, num_tiles,
                                                                                       tseg);
         probe_end(st, GBWT_PROBE_RADIX_SCATTER, (uint64_t)n * 2 * (sizeof(K) + (HAS_VAL ? 4 : 0)));
