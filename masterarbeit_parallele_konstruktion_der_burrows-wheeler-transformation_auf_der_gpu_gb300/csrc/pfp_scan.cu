@@ -38,6 +38,29 @@ struct ScanArgs {
 
 __device__ __forceinline__ uint32_t bget(const uint32_t *w, int i) { return (w[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
 
+// 2^W mod P: a compile-time constant in the specialised kernels (0 for
+// W=5, P=16, where the outgoing byte drops out of the rolling hash).
+__host__ __device__ constexpr uint32_t pow2_mod(int W, int P)
+{
+    uint32_t v = 1;
+    for (int i = 0; i < W; i++) v = (v * 2u) % (uint32_t)P;
+    return v;
+}
+
+// Byte checks of one thread's 16 bytes (K:130-132) on whole 32-bit words.
+__device__ __forceinline__ void check_words(const uint32_t *w, uint32_t hi, bool &bad, bool &small_bad)
+{
+    const uint32_t hi4 = hi * 0x01010101u;
+    uint32_t b = 0, sb = 0;
+#pragma unroll
+    for (int q = 0; q < TS_PER_THREAD / 4; q++) {
+        b |= __vcmpltu4(w[q], 0x02020202u) | __vcmpeq4(w[q], 0xFFFFFFFFu);
+        sb |= __vcmpgtu4(w[q], hi4);
+    }
+    bad = b != 0;
+    small_bad = sb != 0;
+}
+
 // Stage bytes [base, base + TS_TILE + W - 1) of T into s (zero past n).
 __device__ __forceinline__ void stage_tile(const ScanArgs &a, uint8_t *s, size_t base, int halo16)
 {
@@ -80,12 +103,16 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
 
     if (check_bytes) {
         bool bad = false, small_bad = false;
+        if (s0 + TS_PER_THREAD <= a.n) {
+            check_words(w, a.hi, bad, small_bad);
+        } else {
 #pragma unroll
-        for (int j = 0; j < TS_PER_THREAD; j++) {
-            uint32_t c = bget(w, j);
-            if (s0 + j < a.n) {
-                bad |= (c < 2u) || (c == 255u);
-                small_bad |= (c > a.hi);
+            for (int j = 0; j < TS_PER_THREAD; j++) {
+                uint32_t c = bget(w, j);
+                if (s0 + j < a.n) {
+                    bad |= (c < 2u) || (c == 255u);
+                    small_bad |= (c > a.hi);
+                }
             }
         }
         if (bad) atomicOr(a.flags, ERR_BAD_BYTE);
@@ -124,6 +151,11 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
     }
     const uint64_t regmask = (WT > 0 && WT < 8) ? ((1ull << (8 * (WT > 0 ? WT : 1))) - 1ull) : ~0ull;
 
+    // windows j of this thread that may trigger: s0+j >= 1 and s0+j <= last_valid
+    uint32_t range = (last_valid - s0 >= (size_t)TS_PER_THREAD - 1) ? 0xFFFFu
+                                                                    : (1u << (uint32_t)(last_valid - s0 + 1)) - 1u;
+    if (s0 == 0) range &= ~1u;
+    const uint32_t wW = (WT > 0 && PT > 0) ? pow2_mod(WT > 0 ? WT : 1, PT > 0 ? PT : 1) : a.wW;
     uint32_t mask = 0;
 #pragma unroll
     for (int j = 0; j < TS_PER_THREAD; j++) {
@@ -139,15 +171,15 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
                     if (s[sj - base + i] != s_fw[i]) { eq = false; break; }
             }
         }
-        if (sj >= 1 && sj <= last_valid && (h == 0 || eq)) mask |= 1u << j;
+        if (h == 0 || eq) mask |= 1u << j;
         if (j + 1 < TS_PER_THREAD) {
             const uint32_t out = bget(w, j), in = bget(w, j + W);
-            h = (2u * h + in + 256u * P - out * a.wW) % P;
+            h = (2u * h + in + 256u * P - out * wW) % P;
             if (WT > 0 && WT <= 8) reg = ((reg << 8) | in) & regmask;
             else fp = fp * FP_BASE - (uint64_t)out * fp_pow + in;
         }
     }
-    return mask;
+    return mask & range;
 }
 
 template <int WT, int PT, bool WRITE>
@@ -325,6 +357,7 @@ __device__ __forceinline__ uint32_t tile_triggers_batch(const ScanArgs &a, const
         }
     }
     const uint64_t regmask = (WT > 0 && WT < 8) ? ((1ull << (8 * (WT > 0 ? WT : 1))) - 1ull) : ~0ull;
+    const uint32_t wW = (WT > 0 && PT > 0) ? pow2_mod(WT > 0 ? WT : 1, PT > 0 ? PT : 1) : a.wW;
     uint64_t cur = tcur ? __ldg(b.fw + tcur - 1) : 0ull;
 
     uint32_t mask = 0;
@@ -360,7 +393,7 @@ __device__ __forceinline__ uint32_t tile_triggers_batch(const ScanArgs &a, const
         }
         if (j + 1 < TS_PER_THREAD) {
             const uint32_t in = bget(w, j + W);
-            h = (2u * h + in + 256u * P - c * a.wW) % P;
+            h = (2u * h + in + 256u * P - c * wW) % P;
             c1 += (in == 1u) - (pb == 1u);
             if (WT > 0 && WT <= 8) reg = ((reg << 8) | in) & regmask;
             else fp = fp * FP_BASE - (uint64_t)c * fp_pow + in;
