@@ -216,6 +216,7 @@ __global__ void k_emit_prep(Emit e, const uint32_t *pidpc, const uint8_t *T, uin
 // 256 emission slots per CTA; the CTA writes its contiguous output range
 // with consecutive threads on consecutive elements.
 constexpr int EM_T = 256;
+constexpr int EM_PER = 8;          // consecutive elements per thread and chunk
 template <typename E>
 __global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff, const uint32_t *emq,
                                                const uint8_t *emp, const uint32_t *moff, const uint32_t *mb,
@@ -224,6 +225,7 @@ __global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff,
     __shared__ uint32_t s_off[EM_T + 1];
     __shared__ uint32_t s_base[EM_T];
     __shared__ uint8_t s_prev[EM_T];
+    __shared__ E s_out[EM_T * EM_PER];
     const uint32_t t0 = blockIdx.x * EM_T;
     const uint32_t tn = min((uint32_t)EM_T, z - t0);
     if (threadIdx.x < tn) {
@@ -239,17 +241,33 @@ __global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff,
         if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL);
         return;
     }
-    for (uint32_t e = threadIdx.x; e < cnt; e += EM_T) {
-        const uint32_t o = o0 + e;
-        uint32_t lo = 0, hi = tn - 1u;            // last i with s_off[i] <= o
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1u) >> 1;
-            if (s_off[mid] <= o) lo = mid; else hi = mid - 1u;
+    // chunks of EM_T * EM_PER elements: each thread finds the slot of its
+    // first element once and walks forward; the chunk is staged in shared
+    // memory and written with consecutive threads on consecutive elements
+    for (uint32_t cb = 0; cb < cnt; cb += EM_T * EM_PER) {
+        const uint32_t e0 = cb + threadIdx.x * EM_PER;
+        if (e0 < cnt) {
+            const uint32_t o = o0 + e0;
+            uint32_t lo = 0, hi = tn - 1u;            // last slot with s_off <= o
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1u) >> 1;
+                if (s_off[mid] <= o) lo = mid; else hi = mid - 1u;
+            }
+#pragma unroll
+            for (int q = 0; q < EM_PER; q++) {
+                const uint32_t e = e0 + q;
+                if (e >= cnt) break;
+                while (s_off[lo + 1] <= o0 + e) lo++;
+                const uint32_t j = s_base[lo] + (o0 + e - s_off[lo]);
+                uint32_t c = mc[j];
+                if (c == PC_VAR) c = s_prev[lo];
+                s_out[threadIdx.x * EM_PER + q] = ((E)mb[j] << 8) | (E)c;
+            }
         }
-        const uint32_t j = s_base[lo] + (o - s_off[lo]);
-        uint32_t c = mc[j];
-        if (c == PC_VAR) c = s_prev[lo];
-        elem[o] = ((E)mb[j] << 8) | (E)c;
+        __syncthreads();
+        const uint32_t m = min((uint32_t)(EM_T * EM_PER), cnt - cb);
+        for (uint32_t i = threadIdx.x; i < m; i += EM_T) elem[o0 + cb + i] = s_out[i];
+        __syncthreads();
     }
 }
 

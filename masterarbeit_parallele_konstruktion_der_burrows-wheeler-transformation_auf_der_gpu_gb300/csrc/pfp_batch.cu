@@ -176,6 +176,7 @@ __global__ void k_bemit_prep(BatchEmit e, uint32_t *emq, uint32_t *emt, uint8_t 
 
 // 256 slots per CTA; consecutive threads write consecutive elements.
 constexpr int BE_T = 256;
+constexpr int BE_PER = 8;
 template <typename E>
 __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff, const uint32_t *emq,
                                                 const uint32_t *emt, const uint8_t *emp, const uint32_t *pshift,
@@ -189,6 +190,9 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
     __shared__ E s_hi[BE_T];
     __shared__ uint8_t s_prev[BE_T];
     __shared__ uint8_t s_enc[256];
+    __shared__ E s_val[BE_T * BE_PER];
+    __shared__ uint32_t s_dst[BE_T * BE_PER];
+    __shared__ uint32_t s_pos[BE_T * BE_PER];
     const uint32_t t0 = blockIdx.x * BE_T;
     const uint32_t tn = min((uint32_t)BE_T, S - t0);
     s_enc[threadIdx.x] = enc[threadIdx.x];          // blockDim == 256
@@ -203,23 +207,44 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
     if (threadIdx.x == 0) s_off[tn] = eoff[t0 + tn];
     __syncthreads();
     const uint32_t o0 = s_off[0], cnt = s_off[tn] - o0;
-    for (uint32_t i = threadIdx.x; i < cnt; i += BE_T) {
-        const uint32_t o = o0 + i;
-        uint32_t lo = 0, hi = tn - 1u;            // last slot with s_off <= o
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi + 1u) >> 1;
-            if (s_off[mid] <= o) lo = mid; else hi = mid - 1u;
+    // chunks of BE_T * BE_PER elements: each thread searches the slot of its
+    // first element once and walks forward; the chunk is staged in shared
+    // memory and written with consecutive threads on consecutive elements
+    for (uint32_t cb = 0; cb < cnt; cb += BE_T * BE_PER) {
+        const uint32_t e0 = cb + threadIdx.x * BE_PER;
+        if (e0 < cnt) {
+            uint32_t lo = 0, hi = tn - 1u;            // last slot with s_off <= o
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1u) >> 1;
+                if (s_off[mid] <= o0 + e0) lo = mid; else hi = mid - 1u;
+            }
+#pragma unroll
+            for (int q = 0; q < BE_PER; q++) {
+                const uint32_t e = e0 + q;
+                if (e >= cnt) break;
+                const uint32_t o = o0 + e;
+                while (s_off[lo + 1] <= o) lo++;
+                const uint32_t j = o - s_off[lo];
+                const uint32_t pos = s_base[lo] + j;
+                const uint32_t c = j ? dict[pos - 1] : s_prev[lo];
+                const uint32_t k = threadIdx.x * BE_PER + q;
+                s_val[k] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
+                s_dst[k] = o + s_shift[lo];
+                if (epos) s_pos[k] = emx[t0 + lo] + j;     // text-local position of this suffix
+            }
         }
-        const uint32_t j = o - s_off[lo];
-        const uint32_t pos = s_base[lo] + j;
-        const uint32_t c = j ? dict[pos - 1] : s_prev[lo];
-        const uint32_t dst = o + s_shift[lo];
-        if (dst < cap) {
-            elem[dst] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
-            if (epos) epos[dst] = emx[t0 + lo] + j;        // text-local position of this suffix
-        } else {
-            atomicOr(flags, ERR_INTERNAL);
+        __syncthreads();
+        const uint32_t m = min((uint32_t)(BE_T * BE_PER), cnt - cb);
+        for (uint32_t i = threadIdx.x; i < m; i += BE_T) {
+            const uint32_t dst = s_dst[i];
+            if (dst < cap) {
+                elem[dst] = s_val[i];
+                if (epos) epos[dst] = s_pos[i];
+            } else {
+                atomicOr(flags, ERR_INTERNAL);
+            }
         }
+        __syncthreads();
     }
 }
 
