@@ -39,11 +39,17 @@ struct ParseRem {
     uint32_t n;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return n - x; }
 };
-// A batch of parses laid end to end: a suffix ends with its own text.
+// A batch of parses laid end to end: a suffix ends with its own text; the
+// remaining length of every suffix is precomputed (one load per test).
 struct BatchParseRem {
-    const uint32_t *ptid, *zend;
-    __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return zend[ptid[x]] - x; }
+    const uint32_t *remv;
+    __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return remv[x]; }
 };
+__global__ void k_batch_rem(const uint32_t *ptid, const uint32_t *zend, uint32_t z, uint32_t *remv)
+{
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < z) remv[x] = zend[ptid[x]] - x;
+}
 
 __global__ void k_iota(uint32_t *v, uint32_t n)
 {
@@ -842,10 +848,13 @@ void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchTe
     const bool two = tune_parse_key_phrases(st) == 2;
     k_parse_keys_batch<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bt.ptid, z, lb, two, keys);
     after_launch(st);
+    uint32_t *remv = slot<uint32_t>(st, S_TMP0, z);
+    k_batch_rem<<<grid_for(z, 256), 256, 0, st->stream>>>(bt.ptid, bt.zend, z, remv);
+    after_launch(st);
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
     pord.rounds = prefix_doubling(st, z, two ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), two ? 2u : 1u,
-                                  BatchParseRem{bt.ptid, bt.zend}, pord.isa,
+                                  BatchParseRem{remv}, pord.isa,
                                   pord.sa);
 }
 
