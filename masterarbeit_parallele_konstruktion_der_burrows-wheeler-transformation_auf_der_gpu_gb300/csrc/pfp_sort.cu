@@ -274,6 +274,151 @@ __device__ __forceinline__ void warp_sort_regs(uint64_t *key, uint32_t s, uint32
     __syncwarp();
 }
 
+// One group of s members (13..): keys key[0..s) = (isa[x+h]+1) << 32 | local
+// index li, xs[li] = the member's suffix.  Writes, for every sorted slot p,
+// nh[p] = new group head | done bit and perm[p] = li.  Run by one warp.
+template <typename Rem>
+__device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g, const uint32_t *xs, uint32_t h2,
+                                           const Rem &rem, uint32_t *out_nh, uint16_t *out_perm, uint32_t lane,
+                                           bool collect_stats, uint32_t *flags)
+{
+    // Fast paths (groups of a repetitive text's copies): the next ranks
+    // isa[x+h] of a group usually take one value, two values, or one
+    // majority value with a few outliers.  A stable partition in input
+    // order replaces the sort.  One counting pass first: min, max, and
+    // for two candidate values (middle and first member) their counts
+    // and the number of members below them.
+    const uint32_t c1 = (uint32_t)(key[s >> 1] >> 32), c2 = (uint32_t)(key[0] >> 32);
+    uint32_t mn = 0xFFFFFFFFu, mx = 0, n1 = 0, n2 = 0, b1 = 0, b2 = 0;
+    for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+        const uint32_t i = c0 + lane;
+        const bool in = i < s;
+        const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : c1;
+        if (in) {
+            mn = min(mn, k2);
+            mx = max(mx, k2);
+        }
+        n1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c1));
+        n2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c2));
+        b1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c1));
+        b2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c2));
+    }
+    mn = __reduce_min_sync(0xFFFFFFFFu, mn);
+    mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+    const uint32_t mj = n1 >= n2 ? c1 : c2, ne = n1 >= n2 ? n1 : n2, nl = n1 >= n2 ? b1 : b2;
+    if (collect_stats && lane == 0)
+        atomicAdd(flags + 20 + (mn == mx ? 0 : (s - ne <= 32 ? 3 : 2)), s);
+    if (s <= SS_WARPMAX && s - ne <= 32) {
+        // majority members in input order after the nl smaller ones;
+        // outlier j goes to lane j and is ranked by counting
+        uint64_t mine = ~0ull;
+        uint32_t no = 0, re = 0;
+        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+            const uint32_t i = c0 + lane;
+            const bool in = i < s;
+            const uint64_t kk = in ? key[i] : 0ull;
+            const bool me = in && (uint32_t)(kk >> 32) == mj;
+            const unsigned be = __ballot_sync(0xFFFFFFFFu, me);
+            const unsigned bo = __ballot_sync(0xFFFFFFFFu, in && !me);
+            if (me) {
+                const uint32_t pos = nl + re + __popc(be & ((1u << lane) - 1u));
+                const uint32_t li = (uint32_t)kk & 0xFFFFu;
+                const bool done = ne == 1 || rem(xs[li]) <= h2;
+                out_nh[pos] = (g + nl) | (done ? 0x80000000u : 0u);
+                out_perm[pos] = (uint16_t)li;
+            }
+            re += __popc(be);
+            if (bo) {
+                const uint32_t want = lane - no;      // this chunk's outlier for this lane
+                const bool take = lane >= no && want < (uint32_t)__popc(bo);
+                const uint32_t src = take ? (uint32_t)__fns(bo, 0, (int)want + 1) : lane;
+                const uint64_t got = __shfl_sync(0xFFFFFFFFu, kk, src);
+                if (take) mine = got;
+                no += __popc(bo);
+            }
+        }
+        const uint32_t my2 = (uint32_t)(mine >> 32);
+        uint32_t rk = 0, lt2 = 0, eq2 = 0;
+        for (uint32_t q = 0; q < no; q++) {
+            const uint64_t o = __shfl_sync(0xFFFFFFFFu, mine, q);
+            const uint32_t o2 = (uint32_t)(o >> 32);
+            rk += o < mine;
+            lt2 += o2 < my2;
+            eq2 += o2 == my2;
+        }
+        if (lane < no) {
+            const bool above = my2 > mj;
+            const uint32_t pos = above ? rk + ne : rk;
+            const uint32_t li = (uint32_t)mine & 0xFFFFu;
+            const bool done = eq2 == 1 || rem(xs[li]) <= h2;
+            out_nh[pos] = (g + (above ? lt2 + ne : lt2)) | (done ? 0x80000000u : 0u);
+            out_perm[pos] = (uint16_t)li;
+        }
+        return;
+    }
+    // exactly two values, both frequent: stable two-way partition
+    bool two = false;
+    uint32_t cmn = 0;                    // members with the smaller value
+    {
+        bool other = false;
+        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+            const uint32_t i = c0 + lane;
+            const uint32_t k2 = i < s ? (uint32_t)(key[i] >> 32) : mn;
+            other |= (k2 != mn && k2 != mx);
+            cmn += __popc(__ballot_sync(0xFFFFFFFFu, i < s && k2 == mn));
+        }
+        two = !__any_sync(0xFFFFFFFFu, other);
+    }
+    if (two) {
+        uint32_t rmn = 0, rmx = 0;       // running ranks among equal members
+        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+            const uint32_t i = c0 + lane;
+            const bool in = i < s;
+            const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : 0u;
+            const bool lo = in && k2 == mn;
+            const unsigned blo = __ballot_sync(0xFFFFFFFFu, lo), bhi = __ballot_sync(0xFFFFFFFFu, in && !lo);
+            const unsigned lt = (1u << lane) - 1u;
+            if (in) {
+                const uint32_t li = (uint32_t)key[i] & 0xFFFFu;
+                uint32_t pos, nh;
+                bool single;
+                if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = cmn == 1; }
+                else { pos = cmn + rmx + __popc(bhi & lt); nh = g + cmn; single = s - cmn == 1; }
+                const bool done = single || rem(xs[li]) <= h2;
+                out_nh[pos] = nh | (done ? 0x80000000u : 0u);
+                out_perm[pos] = (uint16_t)li;
+            }
+            rmn += __popc(blo);
+            rmx += __popc(bhi);
+        }
+        return;
+    }
+    if (s <= 32) warp_sort_regs<1>(key, s, lane);
+    else if (s <= 64) warp_sort_regs<2>(key, s, lane);
+    else if (s <= 128) warp_sort_regs<4>(key, s, lane);
+    else if (s <= SS_WARPMAX) warp_sort_regs<8>(key, s, lane);
+    // new heads: start of each run of equal key2 (carried across chunks)
+    uint32_t carry = 0;
+    for (uint32_t c0 = 0; c0 < s; c0 += 32) {
+        const uint32_t i = c0 + lane;
+        const bool in = i < s;
+        const uint64_t kk = in ? key[i] : 0ull;
+        const uint32_t k2 = (uint32_t)(kk >> 32);
+        const bool knew = in && (i == 0 || (uint32_t)(key[i - 1] >> 32) != k2);
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, knew);
+        const unsigned upto = bal & (0xFFFFFFFFu >> (31u - lane));
+        const uint32_t gstart = upto ? c0 + 31u - __clz(upto) : carry;
+        if (in) {
+            const bool single = knew && (i + 1 == s || (uint32_t)(key[i + 1] >> 32) != k2);
+            const uint32_t li = (uint32_t)kk & 0xFFFFu;
+            const bool done = single || rem(xs[li]) <= h2;
+            out_nh[i] = (g + gstart) | (done ? 0x80000000u : 0u);
+            out_perm[i] = (uint16_t)li;
+        }
+        carry = __shfl_sync(0xFFFFFFFFu, gstart, 31);
+    }
+}
+
 // key2[a] = isa[x+h] + 1 for every active element (all reads of this round's
 // ranks happen before any update); flags[3] counts groups too large for the
 // shared-memory path.
@@ -425,142 +570,9 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         if (sg >= nsegs) break;
         const uint32_t ss = s_ss[sg], se = s_ss[sg + 1], s = se - ss;
         const uint32_t g = s_sg[sg];
-        uint64_t *key = s_key + ss;
-        // Fast paths (groups of a repetitive text's copies): the next ranks
-        // isa[x+h] of a group usually take one value, two values, or one
-        // majority value with a few outliers.  A stable partition in input
-        // order replaces the sort.  One counting pass first: min, max, and
-        // for two candidate values (middle and first member) their counts
-        // and the number of members below them.
-        const uint32_t c1 = (uint32_t)(key[s >> 1] >> 32), c2 = (uint32_t)(key[0] >> 32);
-        uint32_t mn = 0xFFFFFFFFu, mx = 0, n1 = 0, n2 = 0, b1 = 0, b2 = 0;
-        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
-            const uint32_t i = c0 + lane;
-            const bool in = i < s;
-            const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : c1;
-            if (in) {
-                mn = min(mn, k2);
-                mx = max(mx, k2);
-            }
-            n1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c1));
-            n2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 == c2));
-            b1 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c1));
-            b2 += __popc(__ballot_sync(0xFFFFFFFFu, in && k2 < c2));
-        }
-        mn = __reduce_min_sync(0xFFFFFFFFu, mn);
-        mx = __reduce_max_sync(0xFFFFFFFFu, mx);
-        const uint32_t mj = n1 >= n2 ? c1 : c2, ne = n1 >= n2 ? n1 : n2, nl = n1 >= n2 ? b1 : b2;
-        if (collect_stats && lane == 0)
-            atomicAdd(flags + 20 + (mn == mx ? 0 : (s - ne <= 32 ? 3 : 2)), s);
-        if (s <= SS_WARPMAX && s - ne <= 32) {
-            // majority members in input order after the nl smaller ones;
-            // outlier j goes to lane j and is ranked by counting
-            uint64_t mine = ~0ull;
-            uint32_t no = 0, re = 0;
-            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
-                const uint32_t i = c0 + lane;
-                const bool in = i < s;
-                const uint64_t kk = in ? key[i] : 0ull;
-                const bool me = in && (uint32_t)(kk >> 32) == mj;
-                const unsigned be = __ballot_sync(0xFFFFFFFFu, me);
-                const unsigned bo = __ballot_sync(0xFFFFFFFFu, in && !me);
-                if (me) {
-                    const uint32_t pos = nl + re + __popc(be & ((1u << lane) - 1u));
-                    const uint32_t li = (uint32_t)kk & 0xFFFFu;
-                    const bool done = ne == 1 || rem(s_x[li]) <= h2;
-                    s_nh[ss + pos] = (g + nl) | (done ? 0x80000000u : 0u);
-                    s_perm[ss + pos] = (uint16_t)li;
-                }
-                re += __popc(be);
-                if (bo) {
-                    const uint32_t want = lane - no;      // this chunk's outlier for this lane
-                    const bool take = lane >= no && want < (uint32_t)__popc(bo);
-                    const uint32_t src = take ? (uint32_t)__fns(bo, 0, (int)want + 1) : lane;
-                    const uint64_t got = __shfl_sync(0xFFFFFFFFu, kk, src);
-                    if (take) mine = got;
-                    no += __popc(bo);
-                }
-            }
-            const uint32_t my2 = (uint32_t)(mine >> 32);
-            uint32_t rk = 0, lt2 = 0, eq2 = 0;
-            for (uint32_t q = 0; q < no; q++) {
-                const uint64_t o = __shfl_sync(0xFFFFFFFFu, mine, q);
-                const uint32_t o2 = (uint32_t)(o >> 32);
-                rk += o < mine;
-                lt2 += o2 < my2;
-                eq2 += o2 == my2;
-            }
-            if (lane < no) {
-                const bool above = my2 > mj;
-                const uint32_t pos = above ? rk + ne : rk;
-                const uint32_t li = (uint32_t)mine & 0xFFFFu;
-                const bool done = eq2 == 1 || rem(s_x[li]) <= h2;
-                s_nh[ss + pos] = (g + (above ? lt2 + ne : lt2)) | (done ? 0x80000000u : 0u);
-                s_perm[ss + pos] = (uint16_t)li;
-            }
-            continue;
-        }
-        // exactly two values, both frequent: stable two-way partition
-        bool two = false;
-        uint32_t cmn = 0;                    // members with the smaller value
-        {
-            bool other = false;
-            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
-                const uint32_t i = c0 + lane;
-                const uint32_t k2 = i < s ? (uint32_t)(key[i] >> 32) : mn;
-                other |= (k2 != mn && k2 != mx);
-                cmn += __popc(__ballot_sync(0xFFFFFFFFu, i < s && k2 == mn));
-            }
-            two = !__any_sync(0xFFFFFFFFu, other);
-        }
-        if (two) {
-            uint32_t rmn = 0, rmx = 0;       // running ranks among equal members
-            for (uint32_t c0 = 0; c0 < s; c0 += 32) {
-                const uint32_t i = c0 + lane;
-                const bool in = i < s;
-                const uint32_t k2 = in ? (uint32_t)(key[i] >> 32) : 0u;
-                const bool lo = in && k2 == mn;
-                const unsigned blo = __ballot_sync(0xFFFFFFFFu, lo), bhi = __ballot_sync(0xFFFFFFFFu, in && !lo);
-                const unsigned lt = (1u << lane) - 1u;
-                if (in) {
-                    const uint32_t li = (uint32_t)key[i] & 0xFFFFu;
-                    uint32_t pos, nh;
-                    bool single;
-                    if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = cmn == 1; }
-                    else { pos = cmn + rmx + __popc(bhi & lt); nh = g + cmn; single = s - cmn == 1; }
-                    const bool done = single || rem(s_x[li]) <= h2;
-                    s_nh[ss + pos] = nh | (done ? 0x80000000u : 0u);
-                    s_perm[ss + pos] = (uint16_t)li;
-                }
-                rmn += __popc(blo);
-                rmx += __popc(bhi);
-            }
-            continue;
-        }
-        if (s <= 32) warp_sort_regs<1>(key, s, lane);
-        else if (s <= 64) warp_sort_regs<2>(key, s, lane);
-        else if (s <= 128) warp_sort_regs<4>(key, s, lane);
-        else if (s <= SS_WARPMAX) warp_sort_regs<8>(key, s, lane);
-        // new heads: start of each run of equal key2 (carried across chunks)
-        uint32_t carry = 0;
-        for (uint32_t c0 = 0; c0 < s; c0 += 32) {
-            const uint32_t i = c0 + lane;
-            const bool in = i < s;
-            const uint64_t kk = in ? key[i] : 0ull;
-            const uint32_t k2 = (uint32_t)(kk >> 32);
-            const bool knew = in && (i == 0 || (uint32_t)(key[i - 1] >> 32) != k2);
-            const unsigned bal = __ballot_sync(0xFFFFFFFFu, knew);
-            const unsigned upto = bal & (0xFFFFFFFFu >> (31u - lane));
-            const uint32_t gstart = upto ? c0 + 31u - __clz(upto) : carry;
-            if (in) {
-                const bool single = knew && (i + 1 == s || (uint32_t)(key[i + 1] >> 32) != k2);
-                const uint32_t li = (uint32_t)kk & 0xFFFFu;
-                const bool done = single || rem(s_x[li]) <= h2;
-                s_nh[ss + i] = (g + gstart) | (done ? 0x80000000u : 0u);
-                s_perm[ss + i] = (uint16_t)li;
-            }
-            carry = __shfl_sync(0xFFFFFFFFu, gstart, 31);
-        }
+        // (groups above SS_WARPMAX were sorted by the CTA above; warp_group
+        // derives their heads only)
+        warp_group<Rem>(s_key + ss, s, g, s_x, h2, rem, s_nh + ss, s_perm + ss, lane, collect_stats, flags);
     }
     __syncthreads();
 
@@ -646,7 +658,7 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         after_launch(st);
         check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
         check_cuda(cudaStreamSynchronize(st->stream));
-        const bool big = ((uint32_t)st->h_scalars[2]) != 0;
+        const bool big = ((uint32_t)st->h_scalars[2]) != 0;      // a group above SS_SEGMAX
         if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u path=%s\n", (unsigned long long)h, A,
                            big ? "global" : "segmented");
         if (!big) {
