@@ -57,25 +57,6 @@ __global__ void k_iota(uint32_t *v, uint32_t n)
     if (i < n) v[i] = i;
 }
 
-// Round 0 heads: max-scan of (new key ? t : 0).
-struct LoadKeyHead {
-    const uint64_t *k;
-    __device__ __forceinline__ uint32_t operator()(size_t t) const
-    {
-        return (t == 0 || k[t] != k[t - 1]) ? (uint32_t)t : 0u;
-    }
-};
-struct StoreHead0 {
-    const uint32_t *vals;
-    uint32_t *isa;
-    uint32_t *head;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t h, uint32_t) const
-    {
-        isa[vals[t]] = h;
-        head[t] = h;
-    }
-};
-
 // Active test after a round whose prefix length is now `h`.
 template <typename Rem>
 struct ActiveTest {
@@ -97,22 +78,45 @@ struct LoadActive {
     ActiveTest<Rem> a;
     __device__ __forceinline__ uint32_t operator()(size_t t) const { return a.done(t) ? 0u : 1u; }
 };
-// Compaction of the active elements; finished ones are written to sa[].
-// `pos` gives an element's final position (round 0: t; later rounds: from
-// the head array, see StoreRound).
+// Round 0 after the sort, in one scan of packed pairs: the high word is a
+// max-scan of group starts (an element's group head), the low word counts
+// the active elements before it (its slot in the active list).  Finished
+// elements go straight to their suffix-array slot t.
+struct OpMaxAdd {
+    __device__ __forceinline__ uint64_t operator()(uint64_t a, uint64_t b) const
+    {
+        const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+        return ((uint64_t)(ah > bh ? ah : bh) << 32) | (uint32_t)((uint32_t)a + (uint32_t)b);
+    }
+};
 template <typename Rem>
-struct StoreActive0 {
+struct LoadHeadActive0 {
     ActiveTest<Rem> a;
-    const uint32_t *head;
+    __device__ __forceinline__ uint64_t operator()(size_t t) const
+    {
+        const uint64_t key = a.k[t];
+        const bool first = t == 0 || a.k[t - 1] != key;
+        const bool last = t + 1 == a.n || a.k[t + 1] != key;
+        const bool done = (first && last) || a.rem(a.vals[t]) <= a.h;
+        return ((uint64_t)(first ? (uint32_t)t : 0u) << 32) | (done ? 0u : 1u);
+    }
+};
+template <typename Rem>
+struct StoreHeadActive0 {
+    ActiveTest<Rem> a;
+    uint32_t *isa;
     uint32_t *sa;
     uint32_t *act_x;
     uint32_t *act_g;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t v) const
+    __device__ __forceinline__ void operator()(size_t t, uint64_t pre, uint64_t v) const
     {
         const uint32_t x = a.vals[t];
-        if (v) {
-            act_x[pre] = x;
-            act_g[pre] = head[t];
+        const uint32_t ph = (uint32_t)(pre >> 32), vh = (uint32_t)(v >> 32);
+        const uint32_t h = ph > vh ? ph : vh;          // inclusive max: the group head
+        isa[x] = h;
+        if ((uint32_t)v) {
+            act_x[(uint32_t)pre] = x;
+            act_g[(uint32_t)pre] = h;
         } else {
             sa[t] = x;
         }
@@ -625,19 +629,17 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     uint32_t *act_g = slot<uint32_t>(st, S_ACTG, N);
     uint32_t *act_x2 = slot<uint32_t>(st, S_ACTX2, N);   // next active list (segmented rounds)
     uint32_t *act_g2 = slot<uint32_t>(st, S_ACTG2, N);
-    uint32_t *head = slot<uint32_t>(st, S_HEAD, N);
     int rounds = 1;
 
     k_iota<<<grid_for(N, 256), 256, 0, st->stream>>>(vals, N);
     after_launch(st);
     radix_sort<uint64_t, true>(st, keys, keys_alt, vals, vals_alt, N, 0, key0_bits);
-    device_scan<uint32_t, OpMax>(st, N, LoadKeyHead{keys}, StoreHead0{vals, isa, head}, true, (uint32_t *)nullptr);
     ActiveTest<Rem> at{keys, vals, N, h0, rem};
     check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-    device_scan<uint32_t, OpAdd>(st, N, LoadActive<Rem>{at}, StoreActive0<Rem>{at, head, sa, act_x, act_g}, false,
-                                 (uint32_t *)st->d_scalars);
+    device_scan<uint64_t, OpMaxAdd>(st, N, LoadHeadActive0<Rem>{at}, StoreHeadActive0<Rem>{at, isa, sa, act_x, act_g},
+                                    false, (uint64_t *)st->d_scalars);
     fetch_scalars(st, 1);
-    uint32_t A = (uint32_t)st->h_scalars[0];
+    uint32_t A = (uint32_t)st->h_scalars[0];      // low word of the total: active elements
     const int lb = bits_for(N);          // isa+1 <= N
     const int gb = bits_for(N - 1);
     uint64_t h = h0;
@@ -689,6 +691,7 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
             continue;
         }
         // the key arrays of the previous round are dead: rebuild in place
+        uint32_t *head = slot<uint32_t>(st, S_HEAD, N);
         uint64_t *k = slot<uint64_t>(st, S_KEY0, N);
         uint64_t *k_alt = slot<uint64_t>(st, S_KEY1, N);
         uint32_t *v = slot<uint32_t>(st, S_VAL0, N);
@@ -749,25 +752,37 @@ __global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, const 
     keys[x] = key;
 }
 
-// Dense lexicographic rank of each distinct phrase (positions at offset 0).
-struct LoadIsStart {
-    const uint32_t *sa;
-    const uint32_t *dphr, *doff;
-    __device__ __forceinline__ uint32_t operator()(size_t t) const
-    {
-        uint32_t x = sa[t];
-        return doff[dphr[x]] == x ? 1u : 0u;
-    }
+// Dense lexicographic rank of each distinct phrase.  After the sort, isa[x]
+// is the head of x's group in sa; distinct phrases never share a group, so
+// the phrase starts' heads are distinct and their order is the phrases'
+// order.  The heads are marked in a bit vector over sa positions; a phrase's
+// rank is the number of marks before its head (word popcount prefix plus the
+// popcount inside the word).  That touches d phrases and N/32 words instead
+// of all N dictionary positions.
+__global__ void k_mark_phrase_heads(const uint32_t *isa, const uint32_t *doff, uint32_t d, uint32_t *bits)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= d) return;
+    const uint32_t p = isa[doff[q]];
+    atomicOr(&bits[p >> 5], 1u << (p & 31));
+}
+struct LoadPopc {
+    const uint32_t *bits;
+    __device__ __forceinline__ uint32_t operator()(size_t t) const { return (uint32_t)__popc(bits[t]); }
 };
-struct StoreLexRank {
-    const uint32_t *sa;
-    const uint32_t *dphr;
-    uint32_t *lexrank;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t v) const
-    {
-        if (v) lexrank[dphr[sa[t]]] = pre;
-    }
+struct StoreWordPre {
+    uint32_t *pre;
+    __device__ __forceinline__ void operator()(size_t t, uint32_t p, uint32_t) const { pre[t] = p; }
 };
+__global__ void k_phrase_lexrank(const uint32_t *isa, const uint32_t *doff, uint32_t d, const uint32_t *bits,
+                                 const uint32_t *pre, uint32_t *lexrank)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= d) return;
+    const uint32_t p = isa[doff[q]];
+    const uint32_t w = p >> 5;
+    lexrank[q] = pre[w] + (uint32_t)__popc(bits[w] & ((1u << (p & 31)) - 1u));
+}
 
 void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
 {
@@ -806,8 +821,16 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
     dord.sa = slot<uint32_t>(st, S_SA, N);
     dord.rounds = prefix_doubling(st, N, h0 * bps + 1, (uint32_t)h0, rem, dord.isa, dord.sa);
     dord.lexrank = slot<uint32_t>(st, S_LEXRANK, ph.d);
-    device_scan<uint32_t, OpAdd>(st, N, LoadIsStart{dord.sa, ph.dphr, ph.doff},
-                                 StoreLexRank{dord.sa, ph.dphr, dord.lexrank}, false, (uint32_t *)nullptr);
+    const size_t words = ((size_t)N + 31) / 32;
+    uint32_t *bits = slot<uint32_t>(st, S_TMP0, words);
+    uint32_t *pre = slot<uint32_t>(st, S_TMP2, words);
+    check_cuda(cudaMemsetAsync(bits, 0, words * sizeof(uint32_t), st->stream));
+    k_mark_phrase_heads<<<grid_for(ph.d, 256), 256, 0, st->stream>>>(dord.isa, ph.doff, ph.d, bits);
+    after_launch(st);
+    device_scan<uint32_t, OpAdd>(st, words, LoadPopc{bits}, StoreWordPre{pre}, false, (uint32_t *)nullptr);
+    k_phrase_lexrank<<<grid_for(ph.d, 256), 256, 0, st->stream>>>(dord.isa, ph.doff, ph.d, bits, pre,
+                                                                   dord.lexrank);
+    after_launch(st);
 }
 
 // First parse key: one phrase rank (two == false), or two (the second 0
