@@ -5,6 +5,7 @@ benchmark workloads; the command profilers (ncu) are pointed at.
   python -m <package>.profile_run --workload config2 --scale 0.125 --iters 2
   python -m <package>.profile_run --workload config4 --iters 3            # batched
   python -m <package>.profile_run --workload config4 --per-text --iters 1 # one text per call
+  python -m <package>.profile_run --workload config4 --tuning '{"radix_rank": 2}'
 
 Prints one JSON line with the pipeline counts and per-stage times of the
 last iteration.  Exits non-zero if the BWT is not a permutation of the text.
@@ -29,6 +30,8 @@ def main(argv=None) -> int:
     ap.add_argument("--W", type=int, default=None)
     ap.add_argument("--P", type=int, default=None)
     ap.add_argument("--small", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help='JSON knobs laid over the size class\'s tuning, e.g. \'{"radix_rank": 2}\'')
     args = ap.parse_args(argv)
     import numpy as np
     import torch
@@ -45,6 +48,7 @@ def main(argv=None) -> int:
     do = torch.empty_like(dt)
     torch.cuda.synchronize()
     with pkg.Storage(n) as st:
+        apply_tuning(pkg, st, n, args.tuning)
         for i in range(args.iters):
             st.pfp_bwt_device(dt.data_ptr(), do.data_ptr(), n, W, P, args.small, stage_times=(i == args.iters - 1))
         torch.cuda.synchronize()
@@ -53,9 +57,18 @@ def main(argv=None) -> int:
     if not np.array_equal(np.bincount(out, minlength=256), np.bincount(text, minlength=256)):
         print("profile_run: output is not a permutation of the text", file=sys.stderr)
         return 1
-    stats.update({"workload": args.workload, "scale": args.scale, "n": n, "W": W, "P": P, "small": args.small})
+    stats.update({"workload": args.workload, "scale": args.scale, "n": n, "W": W, "P": P, "small": args.small,
+                  "tuning": args.tuning})
     print(json.dumps(stats))
     return 0
+
+
+def apply_tuning(pkg, st, n: int, override: str | None) -> None:
+    """Size-class knobs (tuning.json) with the JSON `override` laid over them."""
+    if not override:
+        return
+    base = pkg.tuning_for(n, pkg.load_tuning()) or {}
+    st.set_tuning({**base, **json.loads(override)})
 
 
 def run_batched(args, pkg, wl) -> int:
@@ -71,6 +84,7 @@ def run_batched(args, pkg, wl) -> int:
     stream = torch.cuda.current_stream()
     with pkg.Storage(n) as st:
         st.set_stream(stream.cuda_stream)
+        apply_tuning(pkg, st, n, args.tuning)
         ms = []
         for i in range(args.iters):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -91,7 +105,7 @@ def run_batched(args, pkg, wl) -> int:
         print("profile_run: output is not a permutation of the texts", file=sys.stderr)
         return 1
     stats.update({"workload": "config4", "per_text": args.per_text, "scale": args.scale, "n": n,
-                  "texts": len(offsets) - 1, "W": W, "P": P, "ms": [round(x, 3) for x in ms],
+                  "texts": len(offsets) - 1, "W": W, "P": P, "tuning": args.tuning, "ms": [round(x, 3) for x in ms],
                   "MBps_last": round(n / (ms[-1] / 1000) / 1e6, 1)})
     print(json.dumps(stats))
     return 0
