@@ -28,43 +28,88 @@ uint32_t run_trigger_scan_batch(Storage *st, const uint8_t *dX, uint32_t N, int 
                                 uint32_t k, uint32_t *&D);
 
 constexpr int PC_THREADS = 256;
-constexpr uint32_t PC_CHUNK = 16384;      // input bytes per CTA of the padded copy
+constexpr int PC_UNITS = 4;                                  // 16-byte units of X per thread
+constexpr uint32_t PC_XCHUNK = PC_THREADS * PC_UNITS * 16;   // bytes of X per CTA
 
-// X[xstart[t] + i] = Tin[ioff[t] + i]; W sentinel bytes after each text.
-// Consecutive threads copy consecutive bytes (the shift per text is arbitrary).
+// Last text t < k with xstart[t] <= p, searched in [lo, hi].
+__device__ __forceinline__ uint32_t text_of(const uint32_t *xstart, uint32_t lo, uint32_t hi, uint64_t p)
+{
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (xstart[mid] <= p) lo = mid; else hi = mid - 1u;
+    }
+    return lo;
+}
+
+// X[xstart[t] + i] = Tin[ioff[t] + i]; W sentinel bytes after each text,
+// zeros from N on.  Every thread writes aligned 16-byte units of X: a unit
+// inside one text's bytes is four funnel shifts of five 4-byte loads
+// (`words`: Tin 4-byte aligned), units at a text's end go byte by byte.
+// Input bytes are checked on the way (K:130-132).
 __global__ void __launch_bounds__(PC_THREADS) k_pad_copy(const uint8_t *Tin, uint64_t total, const uint32_t *ioff,
                                                          const uint32_t *xstart, uint32_t k, int W, uint32_t hi,
-                                                         uint8_t *X, uint32_t *flags)
+                                                         bool words, uint64_t N, uint8_t *X, uint32_t *flags)
 {
-    __shared__ uint32_t s_t;
-    const uint64_t c0 = (uint64_t)blockIdx.x * PC_CHUNK;
-    const uint64_t c1 = c0 + PC_CHUNK < total ? c0 + PC_CHUNK : total;
-    if (threadIdx.x == 0) {                 // last text with ioff <= c0
-        uint32_t lo = 0, h = k - 1u;
-        while (lo < h) {
-            const uint32_t mid = (lo + h + 1u) >> 1;
-            if (ioff[mid] <= c0) lo = mid; else h = mid - 1u;
-        }
-        s_t = lo;
+    __shared__ uint32_t s_t0, s_t1;
+    const uint64_t c0 = (uint64_t)blockIdx.x * PC_XCHUNK;
+    const uint64_t c1 = c0 + PC_XCHUNK < N ? c0 + PC_XCHUNK : N;
+    if (threadIdx.x == 0) {
+        s_t0 = text_of(xstart, 0, k - 1u, c0);
+        s_t1 = text_of(xstart, 0, k - 1u, c1 - 1u);
     }
     __syncthreads();
-    bool bad = false, small_bad = false;
-    for (uint32_t t = s_t; t < k; t++) {
-        const uint64_t a = ioff[t];
-        if (a >= c1) break;
-        const uint32_t xs = xstart[t];
-        const uint32_t len = xstart[t + 1] - xs - (uint32_t)W;
-        const uint64_t e = a + len;
-        const uint64_t lo = a > c0 ? a : c0, up = e < c1 ? e : c1;
-        for (uint64_t i = lo + threadIdx.x; i < up; i += PC_THREADS) {
-            const uint32_t c = __ldg(Tin + i);
-            bad |= (c < 2u) || (c == 255u);
-            small_bad |= c > hi;
-            X[xs + (uint32_t)(i - a)] = (uint8_t)c;
+    const uint32_t hi4 = hi * 0x01010101u;
+    uint32_t bad = 0, small_bad = 0;
+#pragma unroll
+    for (int u = 0; u < PC_UNITS; u++) {
+        const uint64_t p = c0 + ((uint64_t)u * PC_THREADS + threadIdx.x) * 16u;
+        if (p >= c1) break;
+        uint32_t t = text_of(xstart, s_t0, s_t1, p);
+        uint32_t xs = xstart[t];
+        uint32_t len = xstart[t + 1] - xs - (uint32_t)W;
+        uint32_t o[4];
+        const uint64_t off = p - xs;
+        const uint64_t src = (uint64_t)ioff[t] + off;
+        if (words && off + 16u <= len && (src & ~3ull) + 20u <= total) {
+            const uint32_t *ws = (const uint32_t *)(Tin + (src & ~3ull));
+            const uint32_t sh = (uint32_t)(src & 3u) * 8u;
+            uint32_t w[5];
+#pragma unroll
+            for (int q = 0; q < 5; q++) w[q] = __ldg(ws + q);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                o[q] = __funnelshift_r(w[q], w[q + 1], sh);
+                bad |= __vcmpltu4(o[q], 0x02020202u) | __vcmpeq4(o[q], 0xFFFFFFFFu);
+                small_bad |= __vcmpgtu4(o[q], hi4);
+            }
+        } else {
+            uint8_t b[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const uint64_t x = p + (uint64_t)q;
+                uint32_t c = 0;
+                if (x < N) {
+                    while (t + 1u < k && xstart[t + 1] <= x) {
+                        t++;
+                        xs = xstart[t];
+                        len = xstart[t + 1] - xs - (uint32_t)W;
+                    }
+                    const uint64_t ox = x - xs;
+                    if (ox < len) {
+                        c = __ldg(Tin + ioff[t] + ox);
+                        bad |= (c < 2u) || (c == 255u);
+                        small_bad |= c > hi;
+                    } else {
+                        c = 1u;
+                    }
+                }
+                b[q] = (uint8_t)c;
+            }
+            memcpy(o, b, 16);
         }
-        if (e > c0 && e <= c1 && threadIdx.x < (unsigned)W) X[xs + len + threadIdx.x] = 1;
+        *(uint4 *)(X + p) = make_uint4(o[0], o[1], o[2], o[3]);
     }
-    const bool any_bad = __any_sync(0xFFFFFFFFu, bad), any_small = __any_sync(0xFFFFFFFFu, small_bad);
+    const bool any_bad = __any_sync(0xFFFFFFFFu, bad != 0), any_small = __any_sync(0xFFFFFFFFu, small_bad != 0);
     if ((threadIdx.x & 31u) == 0) {
         if (any_bad) atomicOr(flags, ERR_BAD_BYTE);
         else if (any_small) atomicOr(flags, ERR_SMALL_RANGE);
@@ -450,8 +495,9 @@ int64_t run_batch(Storage *st, const uint8_t *T, const int64_t *offsets, int32_t
     check_cuda(cudaMemsetAsync(st->d_flags, 0, 64 * sizeof(uint32_t), st->stream));
     uint8_t *X = slot<uint8_t>(st, S_BX, (size_t)N + 128);
     check_cuda(cudaMemsetAsync(X + N, 0, 128, st->stream));
-    k_pad_copy<<<grid_for(total, PC_CHUNK), PC_THREADS, 0, st->stream>>>(dT, total, ioff, xstart, kk, W,
-                                                                         small ? 15u : 254u, X, st->d_flags);
+    const bool words = (((uintptr_t)dT) & 3u) == 0;
+    k_pad_copy<<<grid_for(N, PC_XCHUNK), PC_THREADS, 0, st->stream>>>(dT, total, ioff, xstart, kk, W,
+                                                                      small ? 15u : 254u, words, N, X, st->d_flags);
     after_launch(st);
     uint8_t *lastb = slot<uint8_t>(st, S_BLAST, kk);
     k_text_last<<<grid_for(kk, 256), 256, 0, st->stream>>>(X, xstart, kk, W, lastb);

@@ -360,7 +360,48 @@ __device__ __forceinline__ uint32_t tile_triggers_batch(const ScanArgs &a, const
     const uint32_t wW = (WT > 0 && PT > 0) ? pow2_mod(WT > 0 ? WT : 1, PT > 0 ? PT : 1) : a.wW;
     uint64_t cur = tcur ? __ldg(b.fw + tcur - 1) : 0ull;
 
+    // Almost every thread sees no sentinel byte, neither just before its
+    // windows nor in them: no text starts there, no window is forced, and
+    // the test is the single-text one against a fixed first window.
+    const uint32_t nb = (uint32_t)TS_PER_THREAD + (uint32_t)W - 1u;
+    bool clean = prevb != 1u && s0 + nb <= a.n;
+    if (clean) {
+        uint32_t ones = 0;
+#pragma unroll
+        for (int q = 0; q < NV * 4; q++) {
+            if ((uint32_t)q * 4u >= nb) break;
+            uint32_t m = __vcmpeq4(w[q], 0x01010101u);
+            if (nb - (uint32_t)q * 4u < 4u) m &= (1u << (8u * (nb - (uint32_t)q * 4u))) - 1u;
+            ones |= m;
+        }
+        clean = ones == 0;
+    }
     uint32_t mask = 0;
+    if (clean) {
+#pragma unroll
+        for (int j = 0; j < TS_PER_THREAD; j++) {
+            bool eq;
+            if (WT > 0 && WT <= 8) {
+                eq = reg == cur;
+            } else {
+                eq = false;
+                if (fp == cur) {
+                    const uint8_t *f = a.T + __ldg(b.xstart + tcur - 1);
+                    eq = true;
+                    for (int i = 0; i < W; i++)
+                        if (s[s0 + j - base + i] != __ldg(f + i)) { eq = false; break; }
+                }
+            }
+            if (h == 0 || eq) mask |= 1u << j;
+            if (j + 1 < TS_PER_THREAD) {
+                const uint32_t out = bget(w, j), in = bget(w, j + W);
+                h = (2u * h + in + 256u * P - out * wW) % P;
+                if (WT > 0 && WT <= 8) reg = ((reg << 8) | in) & regmask;
+                else fp = fp * FP_BASE - (uint64_t)out * fp_pow + in;
+            }
+        }
+        return mask;
+    }
 #pragma unroll
     for (int j = 0; j < TS_PER_THREAD; j++) {
         const size_t sj = s0 + j;
@@ -419,7 +460,10 @@ __global__ void __launch_bounds__(TS_THREADS) k_trigger_batch(ScanArgs a, BatchS
     const uint32_t o = threadIdx.x * TS_PER_THREAD;
     const uint32_t prevb = threadIdx.x ? s[o - 1] : s_prev;
     uint32_t nst = 0;
-    {
+    const uint4 q4 = *(const uint4 *)(s + o);
+    const uint32_t ones = __vcmpeq4(q4.x, 0x01010101u) | __vcmpeq4(q4.y, 0x01010101u) |
+                          __vcmpeq4(q4.z, 0x01010101u) | __vcmpeq4(q4.w, 0x01010101u);
+    if (prevb == 1u || ones) {        // a text can only start after a sentinel byte
         uint32_t pb = prevb;
 #pragma unroll
         for (int j = 0; j < TS_PER_THREAD; j++) {

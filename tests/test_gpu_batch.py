@@ -121,3 +121,19 @@ def test_batch_one_text_per_segment(storage, orc, wl):
     got = storage.pfp_bwt_batch(texts)
     for i, t in enumerate(texts):
         assert np.array_equal(got[i], orc.sa_bwt(t)), i
+
+
+@pytest.mark.parametrize("shift", [1, 2, 3])
+def test_batch_device_pointers_unaligned(storage, wl, shift):
+    """Texts at an odd device address: the padded copy takes its byte path
+    for every unit and must give the same BWTs."""
+    torch = pytest.importorskip("torch")
+    concat, offsets = wl.batch_texts(12, scale=1 / 32, seed=13 + shift)
+    buf = torch.zeros(len(concat) + 8, dtype=torch.uint8, device="cuda")
+    buf[shift:shift + len(concat)] = torch.from_numpy(concat).cuda()
+    dL = torch.empty(len(concat) + 8, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    storage.pfp_bwt_batch_device(buf.data_ptr() + shift, offsets, dL.data_ptr() + shift)
+    L = dL.cpu().numpy()[shift:shift + len(concat)]
+    want = storage.pfp_bwt_batch([concat[offsets[i]:offsets[i + 1]] for i in range(len(offsets) - 1)])
+    assert np.array_equal(L, np.concatenate(want))
