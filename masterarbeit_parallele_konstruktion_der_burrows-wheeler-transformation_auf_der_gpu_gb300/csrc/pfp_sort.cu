@@ -92,12 +92,13 @@ struct OpMaxAdd {
 template <typename Rem>
 struct LoadHeadActive0 {
     ActiveTest<Rem> a;
+    bool cont_bit;      // key bit 0 = "suffix longer than the key's symbols": no rem() gather
     __device__ __forceinline__ uint64_t operator()(size_t t) const
     {
         const uint64_t key = a.k[t];
         const bool first = t == 0 || a.k[t - 1] != key;
         const bool last = t + 1 == a.n || a.k[t + 1] != key;
-        const bool done = (first && last) || a.rem(a.vals[t]) <= a.h;
+        const bool done = (first && last) || (cont_bit ? (key & 1u) == 0 : a.rem(a.vals[t]) <= a.h);
         return ((uint64_t)(first ? (uint32_t)t : 0u) << 32) | (done ? 0u : 1u);
     }
 };
@@ -616,10 +617,12 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
 }
 
 // Sorts N positions; key0 (in slot S_KEY0) holds the initial keys covering
-// h0 symbols.  Fills isa[N] and sa[N]; returns the number of rounds.
+// h0 symbols; with key0_cont, bit 0 of every initial key tells whether the
+// suffix is longer than h0 (rem > h0).  Fills isa[N] and sa[N]; returns the
+// number of rounds.
 template <typename Rem>
 static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, Rem rem, uint32_t *isa,
-                           uint32_t *sa)
+                           uint32_t *sa, bool key0_cont = false)
 {
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, N);
     uint64_t *keys_alt = slot<uint64_t>(st, S_KEY1, N);
@@ -636,7 +639,8 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     radix_sort<uint64_t, true>(st, keys, keys_alt, vals, vals_alt, N, 0, key0_bits);
     ActiveTest<Rem> at{keys, vals, N, h0, rem};
     check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-    device_scan<uint64_t, OpMaxAdd>(st, N, LoadHeadActive0<Rem>{at}, StoreHeadActive0<Rem>{at, isa, sa, act_x, act_g},
+    device_scan<uint64_t, OpMaxAdd>(st, N, LoadHeadActive0<Rem>{at, key0_cont},
+                                    StoreHeadActive0<Rem>{at, isa, sa, act_x, act_g},
                                     false, (uint64_t *)st->d_scalars);
     fetch_scalars(st, 1);
     uint32_t A = (uint32_t)st->h_scalars[0];      // low word of the total: active elements
@@ -819,7 +823,7 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
     after_launch(st);
     dord.isa = slot<uint32_t>(st, S_ISA, N);
     dord.sa = slot<uint32_t>(st, S_SA, N);
-    dord.rounds = prefix_doubling(st, N, h0 * bps + 1, (uint32_t)h0, rem, dord.isa, dord.sa);
+    dord.rounds = prefix_doubling(st, N, h0 * bps + 1, (uint32_t)h0, rem, dord.isa, dord.sa, true);
     dord.lexrank = slot<uint32_t>(st, S_LEXRANK, ph.d);
     const size_t words = ((size_t)N + 31) / 32;
     uint32_t *bits = slot<uint32_t>(st, S_TMP0, words);
