@@ -82,13 +82,6 @@ struct LoadActive {
 // max-scan of group starts (an element's group head), the low word counts
 // the active elements before it (its slot in the active list).  Finished
 // elements go straight to their suffix-array slot t.
-struct OpMaxAdd {
-    __device__ __forceinline__ uint64_t operator()(uint64_t a, uint64_t b) const
-    {
-        const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
-        return ((uint64_t)(ah > bh ? ah : bh) << 32) | (uint32_t)((uint32_t)a + (uint32_t)b);
-    }
-};
 template <typename Rem>
 struct LoadHeadActive0 {
     ActiveTest<Rem> a;

@@ -20,11 +20,16 @@ constexpr int SC_THREADS = 256;
 constexpr int SC_ITEMS = 16;
 constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
 
+// Scan operators.  diff(inc, ex) returns a value v with op(ex, v) == inc:
+// the item itself for sums, the inclusive prefix for maxima (the scan hands
+// stores that v, see k_scan_down).
 struct OpAdd {
     template <typename T> __device__ __forceinline__ T operator()(T a, T b) const { return a + b; }
+    template <typename T> __device__ __forceinline__ T diff(T inc, T ex) const { return inc - ex; }
 };
 struct OpMax {
     template <typename T> __device__ __forceinline__ T operator()(T a, T b) const { return a > b ? a : b; }
+    template <typename T> __device__ __forceinline__ T diff(T inc, T) const { return inc; }
 };
 // Component-wise max of the two 32-bit halves of a 64-bit word.
 struct OpMax2 {
@@ -32,6 +37,19 @@ struct OpMax2 {
         uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
         uint32_t al = (uint32_t)a, bl = (uint32_t)b;
         return ((uint64_t)(ah > bh ? ah : bh) << 32) | (al > bl ? al : bl);
+    }
+    __device__ __forceinline__ uint64_t diff(uint64_t inc, uint64_t) const { return inc; }
+};
+// High half: max; low half: sum (a running head with a running count).
+struct OpMaxAdd {
+    __device__ __forceinline__ uint64_t operator()(uint64_t a, uint64_t b) const
+    {
+        const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+        return ((uint64_t)(ah > bh ? ah : bh) << 32) | (uint32_t)((uint32_t)a + (uint32_t)b);
+    }
+    __device__ __forceinline__ uint64_t diff(uint64_t inc, uint64_t ex) const
+    {
+        return (inc & 0xFFFFFFFF00000000ull) | (uint32_t)((uint32_t)inc - (uint32_t)ex);
     }
 };
 
@@ -85,12 +103,17 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_reduce(Load load, size_t n,
     if (threadIdx.x == 0) partial[blockIdx.x] = total;
 }
 
+// Stores run in striped order (consecutive threads on consecutive items, so
+// a store functor's writes at i coalesce): the blocked prefixes go back
+// through shared memory.  store(i, prefix, v) gets the exclusive (or
+// inclusive) prefix and v = op.diff(inclusive, exclusive) -- the item's
+// value for sums.
 template <typename T, typename Op, typename Load, typename Store>
 __global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store, size_t n,
                                                           const T *partial, bool inclusive,
                                                           T *total_out)
 {
-    __shared__ T s_tile[SC_TILE];
+    __shared__ T s_tile[SC_TILE + 1];
     __shared__ T s_warp[32];
     Op op;
     size_t base = (size_t)blockIdx.x * SC_TILE;
@@ -109,17 +132,24 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store
         sum = op(sum, v[j]);
     }
     T total;
-    T ex = block_excl_scan<T, Op>(sum, total, op, s_warp);
+    T ex = block_excl_scan<T, Op>(sum, total, op, s_warp);   // ends with a barrier: s_tile is free
     T run = partial ? op(partial[blockIdx.x], ex) : ex;
-    size_t i0 = base + (size_t)threadIdx.x * SC_ITEMS;
+    // exclusive prefixes of the tile's items (items past n add the identity)
 #pragma unroll
     for (int j = 0; j < SC_ITEMS; j++) {
-        size_t i = i0 + j;
+        s_tile[threadIdx.x * SC_ITEMS + j] = run;
+        run = op(run, v[j]);
+    }
+    if (threadIdx.x == SC_THREADS - 1) s_tile[SC_TILE] = run;
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < SC_ITEMS; j++) {
+        const uint32_t li = (uint32_t)j * SC_THREADS + threadIdx.x;
+        const size_t i = base + li;
         if (i < n) {
-            T inc = op(run, v[j]);
-            store(i, inclusive ? inc : run, v[j]);
+            const T exi = s_tile[li], inc = s_tile[li + 1];
+            store(i, inclusive ? inc : exi, op.diff(inc, exi));
             if (total_out && i == n - 1) *total_out = inc;
-            run = inc;
         }
     }
 }
