@@ -32,7 +32,7 @@ enum Slot : int {
     S_ELEM0, S_ELEM1,
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
     S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2, S_LCB, S_LCBMAP,
-    S_BX, S_BMETA, S_BTID, S_BZEND, S_BLAST, S_BCODE,
+    S_BX, S_BMETA, S_BTID, S_BZEND, S_BLAST, S_BCODE, S_SSTART,
     S_NUM
 };
 

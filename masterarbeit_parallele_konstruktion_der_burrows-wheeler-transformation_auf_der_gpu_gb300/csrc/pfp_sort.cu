@@ -189,9 +189,15 @@ constexpr int SS_PER_THREAD = SS_CAP / SS_THREADS;
 constexpr uint32_t SS_WARPMAX = 256;      // larger groups are sorted by the CTA
 constexpr uint32_t SS_COUNTMAX = 12;      // smaller groups rank by counting, unsorted
 constexpr int SS_MISC_WORDS = 8 + 64 + 16; // misc, scan scratch (32 x u64), big-group list
+constexpr int SS_MIDMAX = SS_CAP / (SS_COUNTMAX + 1) + 1;   // groups above SS_COUNTMAX in one CTA
 // keys, x, segment heads, segment starts, slot heads (4 B each), misc,
-// element -> segment and slot -> element (2 B each)
-constexpr size_t SS_SMEM = (size_t)SS_CAP * (8 + 4 + 4 + 4 + 4 + 2 + 2) + SS_MISC_WORDS * 4;
+// element -> segment and slot -> element (2 B each), warp-group list (2 B)
+constexpr size_t SS_SMEM = (size_t)SS_CAP * (8 + 4 + 4 + 4 + 4 + 2 + 2) + SS_MISC_WORDS * 4 + SS_MIDMAX * 2;
+// two CTAs per SM (228 KB of shared memory, 1 KB reserved per CTA)
+static_assert(2 * (SS_SMEM + 1024) <= 228 * 1024, "k_seg_sort must keep two CTAs per SM");
+// a group of at most SS_SEGMAX members cannot cover a whole tile, so every
+// full tile after the first group start holds a group start
+static_assert(SS_SEGMAX <= SS_TILE, "tile starts need groups no longer than a tile");
 
 // Sorts key[0..s) ascending with a bitonic network whose merge steps start
 // with the "flipped" comparator (i, block_end-1-i): every comparator is
@@ -419,25 +425,32 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
 
 // key2[a] = isa[x+h] + 1 for every active element (all reads of this round's
 // ranks happen before any update); flags[3] counts groups too large for the
-// shared-memory path.
+// shared-memory path; tstart[b] = first group start in tile b (SS_TILE
+// active indices; 0xFFFFFFFF before, via memset).
 __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
-                               uint32_t h, uint32_t *key2, uint32_t *flags)
+                               uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart)
 {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= A) return;
-    key2[a] = isa[act_x[a] + h] + 1u;
-    const uint32_t g = act_g[a];
-    const bool gnew = a == 0 || act_g[a - 1] != g;
-    if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
+    bool gnew = false;
+    if (a < A) {
+        key2[a] = isa[act_x[a] + h] + 1u;
+        const uint32_t g = act_g[a];
+        gnew = a == 0 || act_g[a - 1] != g;
+        if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
+    }
+    // a warp's 32 indices lie in one tile (blockDim and SS_TILE multiples of 32)
+    const uint32_t first = __reduce_min_sync(0xFFFFFFFFu, gnew ? a : 0xFFFFFFFFu);
+    if ((threadIdx.x & 31u) == 0 && first != 0xFFFFFFFFu) atomicMin(tstart + first / SS_TILE, first);
 }
 
 template <typename Rem>
 __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__restrict__ act_x,
                                                             const uint32_t *__restrict__ act_g,
-                                                            const uint32_t *__restrict__ key2, uint32_t A, uint32_t h2,
-                                                            Rem rem, uint32_t *isa, uint32_t *sa, uint32_t *out_x,
-                                                            uint32_t *out_g, uint32_t *counter, uint32_t *flags,
-                                                            bool collect_stats)
+                                                            const uint32_t *__restrict__ key2,
+                                                            const uint32_t *__restrict__ tstart, uint32_t A,
+                                                            uint32_t h2, Rem rem, uint32_t *isa, uint32_t *sa,
+                                                            uint32_t *out_x, uint32_t *out_g, uint32_t *counter,
+                                                            uint32_t *flags, bool collect_stats)
 {
     extern __shared__ __align__(16) unsigned char ss_smem[];
     uint64_t *s_key = (uint64_t *)ss_smem;           // (isa[x+h]+1) << 32 | local index
@@ -445,44 +458,48 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     uint32_t *s_sg = s_x + SS_CAP;                   // segment -> group head g
     uint32_t *s_ss = s_sg + SS_CAP;                  // segment -> local start index
     uint32_t *s_nh = s_ss + SS_CAP;                  // sorted slot -> new head | done bit
-    uint32_t *s_misc = s_nh + SS_CAP;                // [0] first start, [1] end, [2] warp counter, [3] big, [4] base
+    uint32_t *s_misc = s_nh + SS_CAP;                // [2] warp counter, [3] big, [4] base, [5] warp groups
     uint64_t *s_scan = (uint64_t *)(s_misc + 8);
     uint32_t *s_big = s_misc + 8 + 64;
     uint16_t *s_seg = (uint16_t *)(s_misc + SS_MISC_WORDS);   // local index -> segment
     uint16_t *s_perm = s_seg + SS_CAP;                        // sorted slot -> local index
+    uint16_t *s_mid = s_perm + SS_CAP;                        // segments above SS_COUNTMAX
 
-    const uint32_t a_lo = blockIdx.x * SS_TILE;
-    const uint32_t a_hi = min(a_lo + (uint32_t)SS_TILE, A);
-    if (threadIdx.x == 0) { s_misc[0] = 0xFFFFFFFFu; s_misc[1] = 0xFFFFFFFFu; }
-    __syncthreads();
-    for (uint32_t a = a_lo + threadIdx.x; a < a_hi; a += SS_THREADS)
-        if (a == 0 || act_g[a - 1] != act_g[a]) atomicMin(&s_misc[0], a);
-    const uint32_t e_lim = min(a_hi + (uint32_t)SS_SEGMAX, A);
-    for (uint32_t a = a_hi + threadIdx.x; a < e_lim; a += SS_THREADS)
-        if (act_g[a - 1] != act_g[a]) atomicMin(&s_misc[1], a);
-    __syncthreads();
-    const uint32_t s0 = s_misc[0];
+    // the CTA's elements: from the first group start in its tile to the
+    // first group start in the next tile (or A)
+    const uint32_t s0 = tstart[blockIdx.x];
     if (s0 == 0xFFFFFFFFu) return;                   // no group starts in this tile
-    uint32_t e1 = s_misc[1];
+    uint32_t e1 = blockIdx.x + 1 < gridDim.x ? tstart[blockIdx.x + 1] : A;
     if (e1 == 0xFFFFFFFFu) {
-        if (e_lim < A) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
+        // only the last tile, partly filled, may lack a start
+        if (blockIdx.x + 2 < gridDim.x) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
         e1 = A;
     }
     const uint32_t cnt = e1 - s0;
+    if (cnt > (uint32_t)SS_CAP) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
 
-    // blocked load: thread t owns local indices [t*SS_PER_THREAD, +SS_PER_THREAD)
+    // coalesced loads into shared memory (s_nh holds the group ids for now)
+#pragma unroll
+    for (int j = 0; j < SS_PER_THREAD; j++) {
+        const uint32_t i = (uint32_t)j * SS_THREADS + threadIdx.x;
+        if (i < cnt) {
+            const uint32_t a = s0 + i;
+            // unique key: (isa[x+h]+1, local index) -- stable, deterministic
+            s_key[i] = ((uint64_t)key2[a] << 32) | i;
+            s_x[i] = act_x[a];
+            s_nh[i] = act_g[a];
+        }
+    }
+    __syncthreads();
+    // blocked: thread t owns local indices [t*SS_PER_THREAD, +SS_PER_THREAD)
     const uint32_t i0 = threadIdx.x * SS_PER_THREAD;
     uint32_t nseg = 0;
     bool gn[SS_PER_THREAD];
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
         const uint32_t i = i0 + j;
-        gn[j] = false;
-        if (i < cnt) {
-            const uint32_t a = s0 + i;
-            gn[j] = i == 0 || act_g[a - 1] != act_g[a];
-            nseg += gn[j];
-        }
+        gn[j] = i < cnt && (i == 0 || s_nh[i - 1] != s_nh[i]);
+        nseg += gn[j];
     }
     uint64_t tot;
     uint32_t seg = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nseg, tot, OpAdd(), s_scan);
@@ -491,15 +508,11 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     for (int j = 0; j < SS_PER_THREAD; j++) {
         const uint32_t i = i0 + j;
         if (i < cnt) {
-            const uint32_t a = s0 + i;
-            if (gn[j]) { s_sg[seg] = act_g[a]; s_ss[seg] = i; seg++; }
-            // unique key: (isa[x+h]+1, local index) -- stable, deterministic
-            s_key[i] = ((uint64_t)key2[a] << 32) | i;
-            s_x[i] = act_x[a];
+            if (gn[j]) { s_sg[seg] = s_nh[i]; s_ss[seg] = i; seg++; }
             s_seg[i] = (uint16_t)(seg - 1);
         }
     }
-    if (threadIdx.x == 0) { s_ss[nsegs] = cnt; s_misc[2] = 0; s_misc[3] = 0; }
+    if (threadIdx.x == 0) { s_ss[nsegs] = cnt; s_misc[2] = 0; s_misc[3] = 0; s_misc[5] = 0; }
     __syncthreads();
 
     // Tier 3: groups larger than SS_WARPMAX are sorted by the whole CTA.
@@ -508,6 +521,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     uint32_t e1c = 0, e2c = 0, e3c = 0;
     for (uint32_t sg = threadIdx.x; sg < nsegs; sg += SS_THREADS) {
         const uint32_t s = s_ss[sg + 1] - s_ss[sg];
+        if (s > SS_COUNTMAX) s_mid[atomicAdd(&s_misc[5], 1u)] = (uint16_t)sg;
         if (s > SS_WARPMAX) { s_big[atomicAdd(&s_misc[3], 1u)] = sg; e3c += s; }
         else if (s > SS_COUNTMAX) e2c += s;
         else e1c += s;
@@ -557,15 +571,13 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     // Tiers 2/3: warps take the larger groups from a shared counter, sort the
     // ones up to SS_WARPMAX, and derive the new heads of all of them.
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nmid = s_misc[5];
     for (;;) {
-        uint32_t sg = 0;
-        if (lane == 0) {
-            do {
-                sg = atomicAdd(&s_misc[2], 1u);
-            } while (sg < nsegs && s_ss[sg + 1] - s_ss[sg] <= SS_COUNTMAX);
-        }
-        sg = __shfl_sync(0xFFFFFFFFu, sg, 0);
-        if (sg >= nsegs) break;
+        uint32_t m = 0;
+        if (lane == 0) m = atomicAdd(&s_misc[2], 1u);
+        m = __shfl_sync(0xFFFFFFFFu, m, 0);
+        if (m >= nmid) break;
+        const uint32_t sg = s_mid[m];
         const uint32_t ss = s_ss[sg], se = s_ss[sg + 1], s = se - ss;
         const uint32_t g = s_sg[sg];
         // (groups above SS_WARPMAX were sorted by the CTA above; warp_group
@@ -586,12 +598,19 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     uint64_t atot;
     uint32_t apre = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nact, atot, OpAdd(), s_scan);
     if (threadIdx.x == 0) s_misc[4] = atot ? atomicAdd(counter, (uint32_t)atot) : 0u;
-    __syncthreads();
-    const uint32_t base = s_misc[4];
+    // active slots (x, new head) staged in slot order; the keys are dead
+    uint2 *s_act = (uint2 *)s_key;
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
         const uint32_t p = i0 + j;
         if (p >= cnt) break;
+        const uint32_t v = s_nh[p];
+        if (!(v >> 31)) s_act[apre++] = make_uint2(s_x[s_perm[p]], v);
+    }
+    __syncthreads();
+    const uint32_t base = s_misc[4];
+    // striped: ranks, finished suffixes, next active list
+    for (uint32_t p = threadIdx.x; p < cnt; p += SS_THREADS) {
         const uint32_t v = s_nh[p];
         const uint32_t nh = v & 0x7FFFFFFFu;
         const uint32_t x = s_x[s_perm[p]];
@@ -599,13 +618,12 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         // isa[x] already holds the old group head (the rank it was made
         // active with); only a changed rank is written
         if (nh != s_sg[sg]) isa[x] = nh;
-        if (v >> 31) {
-            sa[s_sg[sg] + (p - s_ss[sg])] = x;
-        } else {
-            out_x[base + apre] = x;
-            out_g[base + apre] = nh;
-            apre++;
-        }
+        if (v >> 31) sa[s_sg[sg] + (p - s_ss[sg])] = x;
+    }
+    for (uint32_t k = threadIdx.x; k < (uint32_t)atot; k += SS_THREADS) {
+        const uint2 e = s_act[k];
+        out_x[base + k] = e.x;
+        out_g[base + k] = e.y;
     }
 }
 
@@ -651,9 +669,12 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
         // gather this round's keys before any rank changes; count big groups
         uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
+        const uint32_t ss_tiles = grid_for(A, SS_TILE);
+        uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles);
         check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
+        check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4, st->stream));
         k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
-                                                                 st->d_flags);
+                                                                 st->d_flags, tstart);
         after_launch(st);
         check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
         check_cuda(cudaStreamSynchronize(st->stream));
@@ -665,8 +686,8 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
             check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
             if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 8 * sizeof(uint32_t), st->stream));
             probe_begin(st, GBWT_PROBE_SEG_SORT);
-            k_seg_sort<Rem><<<grid_for(A, SS_TILE), SS_THREADS, SS_SMEM, st->stream>>>(
-                act_x, act_g, key2, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags, debug);
+            k_seg_sort<Rem><<<ss_tiles, SS_THREADS, SS_SMEM, st->stream>>>(
+                act_x, act_g, key2, tstart, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags, debug);
             // per active element: read x, group, key (12 B); write its rank and
             // either its next-round (x, group) or its final suffix-array slot (12 B)
             probe_end(st, GBWT_PROBE_SEG_SORT, 24ull * A);
