@@ -306,15 +306,31 @@ __global__ void k_bextract(const E *elem, const uint2 *tseg, const uint2 *tout, 
     const uint2 sg = tseg[b], to = tout[b];
     const uint32_t p0 = (b - sg.x) * (uint32_t)RS_TILE;
     const size_t e0 = (size_t)b * RS_TILE;
-    for (uint32_t j = threadIdx.x; j < (uint32_t)RS_TILE; j += 256) {
+    // four consecutive elements per thread: 16-byte (or 2 x 16-byte) loads
+    for (uint32_t j = threadIdx.x * 4u; j < (uint32_t)RS_TILE; j += 4u * 256u) {
         const uint32_t p = p0 + j;
-        if (p < to.y) {
-            out[to.x + p] = s_dec[(uint32_t)elem[e0 + j] & bmask];
-            // sampled suffix array: row (+1, libcubwt's convention) of every
-            // suffix starting at a multiple of 2^r_log2 (one text per call)
-            if (epos) {
-                const uint32_t q = epos[e0 + j];
-                if ((q & ((1u << r_log2) - 1u)) == 0) aux[q >> r_log2] = p + 1u;
+        if (p >= to.y) break;
+        E v[4];
+        if constexpr (sizeof(E) == 4) {
+            const uint4 w = *(const uint4 *)(elem + e0 + j);
+            memcpy(v, &w, 16);
+        } else {
+            const ulonglong2 w0 = *(const ulonglong2 *)(elem + e0 + j);
+            const ulonglong2 w1 = *(const ulonglong2 *)(elem + e0 + j + 2);
+            memcpy(v, &w0, 16);
+            memcpy((char *)v + 16, &w1, 16);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (p + q < to.y) out[to.x + p + q] = s_dec[(uint32_t)v[q] & bmask];
+        // sampled suffix array: row (+1, libcubwt's convention) of every
+        // suffix starting at a multiple of 2^r_log2 (one text per call)
+        if (epos) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (p + q >= to.y) break;
+                const uint32_t x = epos[e0 + j + q];
+                if ((x & ((1u << r_log2) - 1u)) == 0) aux[x >> r_log2] = p + q + 1u;
             }
         }
     }
