@@ -279,11 +279,26 @@ __global__ void k_mixed_scatter(const E *elem, uint32_t M, const uint32_t *delta
 {
     const uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
     if (i0 >= M) return;
+    E v[4];
+    if (i0 + 4u <= M) {                 // one (or two) 16-byte loads
+        if constexpr (sizeof(E) == 4) {
+            const uint4 w = *(const uint4 *)(elem + i0);
+            memcpy(v, &w, 16);
+        } else {
+            const ulonglong2 w0 = *(const ulonglong2 *)(elem + i0);
+            const ulonglong2 w1 = *(const ulonglong2 *)(elem + i0 + 2);
+            memcpy(v, &w0, 16);
+            memcpy((char *)v + 16, &w1, 16);
+        }
+    } else {
+#pragma unroll
+        for (uint32_t j = 0; j < 4; j++) v[j] = i0 + j < M ? elem[i0 + j] : (E)0;
+    }
 #pragma unroll
     for (uint32_t j = 0; j < 4; j++) {
         const uint32_t i = i0 + j;
         if (i >= M) break;
-        const E e = elem[i];
+        const E e = v[j];
         const uint32_t b = (uint32_t)(e >> 8);
         const uint32_t p = b < B ? i + delta[b] : 0xFFFFFFFFu;
         if (p < n) out[p] = (uint8_t)(e & 0xFFu);

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     const uint32_t sa = k0 ? a.D[k0 - 1] - (uint32_t)a.W + 1u : 0u;
     const uint32_t sb = a.D[klast];
     const uint32_t a_al = sa & ~15u;
-    // +32: the word reads of the last chunk may touch 8 bytes past the span
+    // +32: the word reads of the last chunk may touch 12 bytes past the span
     const bool staged = (size_t)(sb - a_al) + 32 <= PH_SPAN;
     if (staged) {
         const bool aligned = (((uintptr_t)a.T) & 15u) == 0;
@@ -93,21 +93,24 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     uint32_t start, end;
     phrase_span(a.D, k, a.W, a.xsep, start, end);
     const uint32_t len = end - start + 1u;
-    // polynomial over little-endian 4-byte chunks (the last one zero-padded)
+    // polynomial mod 2^61-1 over little-endian 7-byte chunks (56 bits, below
+    // the modulus; the last one zero-padded)
     uint64_t h = 0;
     if (staged) {
         const uint32_t *w = (const uint32_t *)s_txt;
-        for (uint32_t i = 0; i < len; i += 4) {
-            const uint32_t p = start - a_al + i;
-            uint32_t chunk = __funnelshift_r(w[p >> 2], w[(p >> 2) + 1], (p & 3u) * 8u);
-            if (len - i < 4) chunk &= (1u << (8u * (len - i))) - 1u;
+        for (uint32_t i = 0; i < len; i += 7) {
+            const uint32_t p = start - a_al + i, q = p >> 2, sh = (p & 3u) * 8u;
+            const uint32_t lo = __funnelshift_r(w[q], w[q + 1], sh), hi = __funnelshift_r(w[q + 1], w[q + 2], sh);
+            uint64_t chunk = (((uint64_t)hi << 32) | lo) & 0x00FFFFFFFFFFFFFFull;
+            if (len - i < 7) chunk &= (1ull << (8u * (len - i))) - 1ull;
             h = mulmod61(h, a.base) + chunk + 1u;
             if (h >= M61) h -= M61;
         }
     } else {
-        for (uint32_t i = 0; i < len; i += 4) {
-            uint32_t chunk = 0;
-            for (uint32_t b = 0; b < 4 && i + b < len; b++) chunk |= (uint32_t)text_at(a.T, a.n, start + i + b) << (8 * b);
+        for (uint32_t i = 0; i < len; i += 7) {
+            uint64_t chunk = 0;
+            for (uint32_t b = 0; b < 7 && i + b < len; b++)
+                chunk |= (uint64_t)text_at(a.T, a.n, start + i + b) << (8 * b);
             h = mulmod61(h, a.base) + chunk + 1u;
             if (h >= M61) h -= M61;
         }
