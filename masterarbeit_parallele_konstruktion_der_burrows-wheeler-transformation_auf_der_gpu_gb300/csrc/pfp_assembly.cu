@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff,
     __shared__ uint32_t s_off[EM_T + 1];
     __shared__ uint32_t s_base[EM_T];
     __shared__ uint8_t s_prev[EM_T];
-    __shared__ E s_out[EM_T * EM_PER];
+    __shared__ E s_out[EM_T * EM_PER + EM_T * EM_PER / 32];     // sc_pad layout (bank-conflict free)
     const uint32_t t0 = blockIdx.x * EM_T;
     const uint32_t tn = min((uint32_t)EM_T, z - t0);
     if (threadIdx.x < tn) {
@@ -261,12 +261,12 @@ __global__ void __launch_bounds__(EM_T) k_emit(uint32_t z, const uint32_t *eoff,
                 const uint32_t j = s_base[lo] + (o0 + e - s_off[lo]);
                 uint32_t c = mc[j];
                 if (c == PC_VAR) c = s_prev[lo];
-                s_out[threadIdx.x * EM_PER + q] = ((E)mb[j] << 8) | (E)c;
+                s_out[sc_pad(threadIdx.x * EM_PER + q)] = ((E)mb[j] << 8) | (E)c;
             }
         }
         __syncthreads();
         const uint32_t m = min((uint32_t)(EM_T * EM_PER), cnt - cb);
-        for (uint32_t i = threadIdx.x; i < m; i += EM_T) elem[o0 + cb + i] = s_out[i];
+        for (uint32_t i = threadIdx.x; i < m; i += EM_T) elem[o0 + cb + i] = s_out[sc_pad(i)];
         __syncthreads();
     }
 }

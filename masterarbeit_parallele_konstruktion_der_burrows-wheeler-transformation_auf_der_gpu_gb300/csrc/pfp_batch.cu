@@ -235,9 +235,10 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
     __shared__ E s_hi[BE_T];
     __shared__ uint8_t s_prev[BE_T];
     __shared__ uint8_t s_enc[256];
-    __shared__ E s_val[BE_T * BE_PER];
-    __shared__ uint32_t s_dst[BE_T * BE_PER];
-    __shared__ uint32_t s_pos[BE_T * BE_PER];
+    // staged chunk in the sc_pad layout (bank-conflict free for both orders)
+    __shared__ E s_val[BE_T * BE_PER + BE_T * BE_PER / 32];
+    __shared__ uint32_t s_dst[BE_T * BE_PER + BE_T * BE_PER / 32];
+    __shared__ uint32_t s_pos[BE_T * BE_PER + BE_T * BE_PER / 32];
     const uint32_t t0 = blockIdx.x * BE_T;
     const uint32_t tn = min((uint32_t)BE_T, S - t0);
     s_enc[threadIdx.x] = enc[threadIdx.x];          // blockDim == 256
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
                 const uint32_t j = o - s_off[lo];
                 const uint32_t pos = s_base[lo] + j;
                 const uint32_t c = j ? dict[pos - 1] : s_prev[lo];
-                const uint32_t k = threadIdx.x * BE_PER + q;
+                const uint32_t k = sc_pad(threadIdx.x * BE_PER + q);
                 s_val[k] = s_hi[lo] | ((E)grp_of[pos] << bb) | (E)s_enc[c];
                 s_dst[k] = o + s_shift[lo];
                 if (epos) s_pos[k] = emx[t0 + lo] + j;     // text-local position of this suffix
@@ -281,10 +282,11 @@ __global__ void __launch_bounds__(BE_T) k_bemit(uint32_t S, const uint32_t *eoff
         __syncthreads();
         const uint32_t m = min((uint32_t)(BE_T * BE_PER), cnt - cb);
         for (uint32_t i = threadIdx.x; i < m; i += BE_T) {
-            const uint32_t dst = s_dst[i];
+            const uint32_t k = sc_pad(i);
+            const uint32_t dst = s_dst[k];
             if (dst < cap) {
-                elem[dst] = s_val[i];
-                if (epos) epos[dst] = s_pos[i];
+                elem[dst] = s_val[k];
+                if (epos) epos[dst] = s_pos[k];
             } else {
                 atomicOr(flags, ERR_INTERNAL);
             }

@@ -491,26 +491,34 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         }
     }
     __syncthreads();
-    // blocked: thread t owns local indices [t*SS_PER_THREAD, +SS_PER_THREAD)
-    const uint32_t i0 = threadIdx.x * SS_PER_THREAD;
-    uint32_t nseg = 0;
-    bool gn[SS_PER_THREAD];
+    // segments in element order, warp-striped: warp w owns local indices
+    // [w*256, w*256+256) as 8 rows of 32 lanes (ballots give the order
+    // inside a row; consecutive lanes touch consecutive banks)
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t wb = (threadIdx.x >> 5) * (32u * SS_PER_THREAD);
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned rowm[SS_PER_THREAD];
+    uint32_t wcnt = 0;
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
-        const uint32_t i = i0 + j;
-        gn[j] = i < cnt && (i == 0 || s_nh[i - 1] != s_nh[i]);
-        nseg += gn[j];
+        const uint32_t i = wb + (uint32_t)j * 32u + lane;
+        rowm[j] = __ballot_sync(0xFFFFFFFFu, i < cnt && (i == 0 || s_nh[i - 1] != s_nh[i]));
+        wcnt += __popc(rowm[j]);
     }
     uint64_t tot;
-    uint32_t seg = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nseg, tot, OpAdd(), s_scan);
+    uint32_t run = (uint32_t)block_excl_scan<uint64_t, OpAdd>(lane == 0 ? (uint64_t)wcnt : 0ull, tot, OpAdd(), s_scan);
+    run = __shfl_sync(0xFFFFFFFFu, run, 0);
     const uint32_t nsegs = (uint32_t)tot;
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
-        const uint32_t i = i0 + j;
+        const uint32_t i = wb + (uint32_t)j * 32u + lane;
         if (i < cnt) {
-            if (gn[j]) { s_sg[seg] = s_nh[i]; s_ss[seg] = i; seg++; }
-            s_seg[i] = (uint16_t)(seg - 1);
+            const uint32_t start = (rowm[j] >> lane) & 1u;
+            const uint32_t sidx = run + (uint32_t)__popc(rowm[j] & lt) + start - 1u;   // segment of i
+            if (start) { s_sg[sidx] = s_nh[i]; s_ss[sidx] = i; }
+            s_seg[i] = (uint16_t)sidx;
         }
+        run += (uint32_t)__popc(rowm[j]);
     }
     if (threadIdx.x == 0) { s_ss[nsegs] = cnt; s_misc[2] = 0; s_misc[3] = 0; s_misc[5] = 0; }
     __syncthreads();
@@ -548,7 +556,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     // the smaller keys of its group (no sort at all) and records its slot.
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
-        const uint32_t i = i0 + j;
+        const uint32_t i = (uint32_t)j * SS_THREADS + threadIdx.x;
         if (i >= cnt) break;
         const uint32_t sg = s_seg[i];
         const uint32_t ss = s_ss[sg], se = s_ss[sg + 1];
@@ -570,7 +578,6 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
 
     // Tiers 2/3: warps take the larger groups from a shared counter, sort the
     // ones up to SS_WARPMAX, and derive the new heads of all of them.
-    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t nmid = s_misc[5];
     for (;;) {
         uint32_t m = 0;
@@ -589,23 +596,27 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     // Final pass over sorted slots: ranks, finished suffixes, and the CTA's
     // share of the next active list (reserved with one atomic; the order of
     // groups in that list does not matter, only each group being contiguous).
-    uint32_t nact = 0;
+    // Active slots are counted warp-striped like the segments above.
+    unsigned actm[SS_PER_THREAD];
+    uint32_t wact = 0;
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
-        const uint32_t p = i0 + j;
-        if (p < cnt) nact += (s_nh[p] >> 31) ^ 1u;
+        const uint32_t p = wb + (uint32_t)j * 32u + lane;
+        actm[j] = __ballot_sync(0xFFFFFFFFu, p < cnt && !(s_nh[p] >> 31));
+        wact += __popc(actm[j]);
     }
     uint64_t atot;
-    uint32_t apre = (uint32_t)block_excl_scan<uint64_t, OpAdd>((uint64_t)nact, atot, OpAdd(), s_scan);
+    uint32_t apre = (uint32_t)block_excl_scan<uint64_t, OpAdd>(lane == 0 ? (uint64_t)wact : 0ull, atot, OpAdd(),
+                                                              s_scan);
+    apre = __shfl_sync(0xFFFFFFFFu, apre, 0);
     if (threadIdx.x == 0) s_misc[4] = atot ? atomicAdd(counter, (uint32_t)atot) : 0u;
     // active slots (x, new head) staged in slot order; the keys are dead
     uint2 *s_act = (uint2 *)s_key;
 #pragma unroll
     for (int j = 0; j < SS_PER_THREAD; j++) {
-        const uint32_t p = i0 + j;
-        if (p >= cnt) break;
-        const uint32_t v = s_nh[p];
-        if (!(v >> 31)) s_act[apre++] = make_uint2(s_x[s_perm[p]], v);
+        const uint32_t p = wb + (uint32_t)j * 32u + lane;
+        if ((actm[j] >> lane) & 1u) s_act[apre + (uint32_t)__popc(actm[j] & lt)] = make_uint2(s_x[s_perm[p]], s_nh[p]);
+        apre += (uint32_t)__popc(actm[j]);
     }
     __syncthreads();
     const uint32_t base = s_misc[4];

@@ -108,12 +108,16 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_reduce(Load load, size_t n,
 // through shared memory.  store(i, prefix, v) gets the exclusive (or
 // inclusive) prefix and v = op.diff(inclusive, exclusive) -- the item's
 // value for sums.
+// Shared-memory slot of tile item i: one padding slot per 32 items, so the
+// blocked accesses (thread t, items 16t..16t+15) hit distinct banks.
+__device__ __forceinline__ uint32_t sc_pad(uint32_t i) { return i + (i >> 5); }
+
 template <typename T, typename Op, typename Load, typename Store>
 __global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store, size_t n,
                                                           const T *partial, bool inclusive,
                                                           T *total_out)
 {
-    __shared__ T s_tile[SC_TILE + 1];
+    __shared__ T s_tile[SC_TILE + SC_TILE / 32 + 1];
     __shared__ T s_warp[32];
     Op op;
     size_t base = (size_t)blockIdx.x * SC_TILE;
@@ -121,14 +125,14 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store
 #pragma unroll 4
     for (int j = 0; j < SC_ITEMS; j++) {
         size_t i = base + (size_t)j * SC_THREADS + threadIdx.x;
-        s_tile[j * SC_THREADS + threadIdx.x] = i < n ? load(i) : T(0);
+        s_tile[sc_pad(j * SC_THREADS + threadIdx.x)] = i < n ? load(i) : T(0);
     }
     __syncthreads();
     T v[SC_ITEMS];
     T sum = T(0);
 #pragma unroll
     for (int j = 0; j < SC_ITEMS; j++) {
-        v[j] = s_tile[threadIdx.x * SC_ITEMS + j];
+        v[j] = s_tile[sc_pad(threadIdx.x * SC_ITEMS + j)];
         sum = op(sum, v[j]);
     }
     T total;
@@ -137,17 +141,17 @@ __global__ void __launch_bounds__(SC_THREADS) k_scan_down(Load load, Store store
     // exclusive prefixes of the tile's items (items past n add the identity)
 #pragma unroll
     for (int j = 0; j < SC_ITEMS; j++) {
-        s_tile[threadIdx.x * SC_ITEMS + j] = run;
+        s_tile[sc_pad(threadIdx.x * SC_ITEMS + j)] = run;
         run = op(run, v[j]);
     }
-    if (threadIdx.x == SC_THREADS - 1) s_tile[SC_TILE] = run;
+    if (threadIdx.x == SC_THREADS - 1) s_tile[sc_pad(SC_TILE)] = run;
     __syncthreads();
 #pragma unroll 4
     for (int j = 0; j < SC_ITEMS; j++) {
         const uint32_t li = (uint32_t)j * SC_THREADS + threadIdx.x;
         const size_t i = base + li;
         if (i < n) {
-            const T exi = s_tile[li], inc = s_tile[li + 1];
+            const T exi = s_tile[sc_pad(li)], inc = s_tile[sc_pad(li + 1)];
             store(i, inclusive ? inc : exi, op.diff(inc, exi));
             if (total_out && i == n - 1) *total_out = inc;
         }
