@@ -324,22 +324,16 @@ __global__ void __launch_bounds__(RF_THREADS) k_run_fill(uint8_t *out, uint32_t 
                                                          const uint16_t *gchar, const uint8_t *gmix,
                                                          const uint32_t *tile_first)
 {
-    __shared__ uint32_t s_off[RF_TILE + 2];
-    __shared__ uint8_t s_chr[RF_TILE + 2];
-    __shared__ uint32_t s_lo, s_hi;
+    __shared__ uint32_t s_off[RF_TILE + 3];
+    __shared__ uint8_t s_chr[RF_TILE + 3];
     const uint32_t base = blockIdx.x * RF_TILE;
     const uint32_t tile_end = min(base + RF_TILE, n);    // exclusive
-    if (threadIdx.x == 0) {
-        s_lo = tile_first[blockIdx.x];
-        uint32_t hi = G - 1u;                            // group containing tile_end - 1
-        if (tile_end < n) {
-            hi = tile_first[blockIdx.x + 1];
-            if (goff[hi] == tile_end) hi--;
-        }
-        s_hi = hi;
-    }
-    __syncthreads();
-    const uint32_t glo = s_lo, m = s_hi - s_lo + 1u;   // m <= RF_TILE
+    // groups glo .. glo+m-1 cover the tile: from the group containing its first
+    // byte to the one containing tile_end (one group too many when that one
+    // starts exactly at tile_end; it is never selected), m <= RF_TILE + 1
+    const uint32_t glo = tile_first[blockIdx.x];
+    const uint32_t ghi = tile_end < n ? tile_first[blockIdx.x + 1] : G - 1u;
+    const uint32_t m = ghi - glo + 1u;
     for (uint32_t i = threadIdx.x; i <= m; i += RF_THREADS) {
         s_off[i] = goff[glo + i];      // goff[G] == n exists
         if (i < m) s_chr[i] = gmix[glo + i] ? 0 : (uint8_t)gchar[glo + i];
