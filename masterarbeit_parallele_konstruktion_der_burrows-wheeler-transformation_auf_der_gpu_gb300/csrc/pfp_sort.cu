@@ -27,6 +27,8 @@
 
 namespace gbwt {
 
+// Remaining length of the suffix at x (rem(x)) and the test ends(x, h) =
+// rem(x) <= h: the suffix is fully compared once its first h symbols are.
 struct DictRem {
     const uint32_t *dphr, *doff, *dlen;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const
@@ -34,21 +36,52 @@ struct DictRem {
         uint32_t q = dphr[x];
         return doff[q] + dlen[q] - x;
     }
+    __device__ __forceinline__ bool ends(uint32_t x, uint32_t h) const { return (*this)(x) <= h; }
 };
 struct ParseRem {
     uint32_t n;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return n - x; }
+    __device__ __forceinline__ bool ends(uint32_t x, uint32_t h) const { return n - x <= h; }
 };
 // A batch of parses laid end to end: a suffix ends with its own text; the
-// remaining length of every suffix is precomputed (one load per test).
+// remaining length of every suffix is precomputed.  ends(x, h) first asks a
+// bitmap of 64-position blocks holding a text's last position (L1-sized):
+// when no block of [x, x+h-1] holds one, the text of x goes on past x+h-1
+// and the remaining length is not loaded.
+constexpr uint32_t BR_MAPH = 1024;      // longest range the bitmap answers
 struct BatchParseRem {
     const uint32_t *remv;
+    const uint32_t *endmap;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return remv[x]; }
+    __device__ __forceinline__ bool ends(uint32_t x, uint32_t h) const
+    {
+        if (h == 0) return false;
+        if (h <= BR_MAPH && x <= 0xFFFFFFFFu - BR_MAPH) {
+            const uint32_t b0 = x >> 6, b1 = (x + h - 1u) >> 6;       // b1 - b0 <= 16
+            const uint32_t w0 = b0 >> 5, w1 = b1 >> 5;
+            uint32_t m = __ldg(endmap + w0) >> (b0 & 31u);
+            if (w0 == w1) {
+                m &= 0xFFFFFFFFu >> (31u - (b1 - b0));
+            } else if (!m) {
+                m = __ldg(endmap + w1) & (0xFFFFFFFFu >> (31u - (b1 & 31u)));
+            }
+            if (!m) return false;
+        }
+        return remv[x] <= h;
+    }
 };
 __global__ void k_batch_rem(const uint32_t *ptid, const uint32_t *zend, uint32_t z, uint32_t *remv)
 {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x < z) remv[x] = zend[ptid[x]] - x;
+}
+// Bit b of endmap: some text's last parse position lies in [64b, 64b+64).
+__global__ void k_text_endmap(const uint32_t *zend, uint32_t k, uint32_t *endmap)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    const uint32_t e = zend[t] - 1u;
+    atomicOr(endmap + (e >> 11), 1u << ((e >> 6) & 31u));
 }
 
 __global__ void k_iota(uint32_t *v, uint32_t n)
@@ -69,7 +102,7 @@ struct ActiveTest {
     {
         const uint64_t key = k[t];
         const bool single = (t == 0 || k[t - 1] != key) && (t + 1 == n || k[t + 1] != key);
-        return single || rem(vals[t]) <= h;
+        return single || rem.ends(vals[t], h);
     }
 };
 
@@ -91,7 +124,7 @@ struct LoadHeadActive0 {
         const uint64_t key = a.k[t];
         const bool first = t == 0 || a.k[t - 1] != key;
         const bool last = t + 1 == a.n || a.k[t + 1] != key;
-        const bool done = (first && last) || (cont_bit ? (key & 1u) == 0 : a.rem(a.vals[t]) <= a.h);
+        const bool done = (first && last) || (cont_bit ? (key & 1u) == 0 : a.rem.ends(a.vals[t], a.h));
         return ((uint64_t)(first ? (uint32_t)t : 0u) << 32) | (done ? 0u : 1u);
     }
 };
@@ -327,7 +360,7 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
             if (me) {
                 const uint32_t pos = nl + re + __popc(be & ((1u << lane) - 1u));
                 const uint32_t li = (uint32_t)kk & 0xFFFFu;
-                const bool done = ne == 1 || rem(xs[li]) <= h2;
+                const bool done = ne == 1 || rem.ends(xs[li], h2);
                 out_nh[pos] = (g + nl) | (done ? 0x80000000u : 0u);
                 out_perm[pos] = (uint16_t)li;
             }
@@ -354,7 +387,7 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
             const bool above = my2 > mj;
             const uint32_t pos = above ? rk + ne : rk;
             const uint32_t li = (uint32_t)mine & 0xFFFFu;
-            const bool done = eq2 == 1 || rem(xs[li]) <= h2;
+            const bool done = eq2 == 1 || rem.ends(xs[li], h2);
             out_nh[pos] = (g + (above ? lt2 + ne : lt2)) | (done ? 0x80000000u : 0u);
             out_perm[pos] = (uint16_t)li;
         }
@@ -388,7 +421,7 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
                 bool single;
                 if (lo) { pos = rmn + __popc(blo & lt); nh = g; single = cmn == 1; }
                 else { pos = cmn + rmx + __popc(bhi & lt); nh = g + cmn; single = s - cmn == 1; }
-                const bool done = single || rem(xs[li]) <= h2;
+                const bool done = single || rem.ends(xs[li], h2);
                 out_nh[pos] = nh | (done ? 0x80000000u : 0u);
                 out_perm[pos] = (uint16_t)li;
             }
@@ -415,7 +448,7 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
         if (in) {
             const bool single = knew && (i + 1 == s || (uint32_t)(key[i + 1] >> 32) != k2);
             const uint32_t li = (uint32_t)kk & 0xFFFFu;
-            const bool done = single || rem(xs[li]) <= h2;
+            const bool done = single || rem.ends(xs[li], h2);
             out_nh[i] = (g + gstart) | (done ? 0x80000000u : 0u);
             out_perm[i] = (uint16_t)li;
         }
@@ -571,7 +604,7 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
             eq += o2 == k2;
             pos += o < kk;
         }
-        const bool done = eq == 1 || rem(s_x[i]) <= h2;
+        const bool done = eq == 1 || rem.ends(s_x[i], h2);
         s_nh[ss + pos] = (s_sg[sg] + lt) | (done ? 0x80000000u : 0u);
         s_perm[ss + pos] = (uint16_t)i;
     }
@@ -915,11 +948,16 @@ void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchTe
     uint32_t *remv = slot<uint32_t>(st, S_TMP0, z);
     k_batch_rem<<<grid_for(z, 256), 256, 0, st->stream>>>(bt.ptid, bt.zend, z, remv);
     after_launch(st);
+    // bitmap words for positions up to z + BR_MAPH (ranges reach past z)
+    const size_t map_words = ((size_t)z + BR_MAPH + 64u * 32u) / (64u * 32u) + 1u;
+    uint32_t *endmap = slot<uint32_t>(st, S_TMP1, map_words);
+    check_cuda(cudaMemsetAsync(endmap, 0, map_words * 4, st->stream));
+    k_text_endmap<<<grid_for(bt.k, 256), 256, 0, st->stream>>>(bt.zend, bt.k, endmap);
+    after_launch(st);
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
     pord.rounds = prefix_doubling(st, z, two ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), two ? 2u : 1u,
-                                  BatchParseRem{remv}, pord.isa,
-                                  pord.sa);
+                                  BatchParseRem{remv, endmap}, pord.isa, pord.sa);
 }
 
 }  // namespace gbwt
