@@ -29,15 +29,24 @@ namespace gbwt {
 
 // Remaining length of the suffix at x (rem(x)) and the test ends(x, h) =
 // rem(x) <= h: the suffix is fully compared once its first h symbols are.
+// Dictionary suffixes end with their phrase; rem8[x] = min(rem(x), 255) (one
+// byte per position, L2-resident) answers ends() for h < 255 without the
+// phrase-table lookups.
 struct DictRem {
     const uint32_t *dphr, *doff, *dlen;
+    const uint8_t *rem8;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const
     {
         uint32_t q = dphr[x];
         return doff[q] + dlen[q] - x;
     }
-    __device__ __forceinline__ bool ends(uint32_t x, uint32_t h) const { return (*this)(x) <= h; }
+    __device__ __forceinline__ bool ends(uint32_t x, uint32_t h) const
+    {
+        if (rem8 && h < 255u) return rem8[x] <= h;
+        return (*this)(x) <= h;
+    }
 };
+
 struct ParseRem {
     uint32_t n;
     __device__ __forceinline__ uint32_t operator()(uint32_t x) const { return n - x; }
@@ -799,8 +808,9 @@ __global__ void k_alpha_present(const uint8_t *dict, uint32_t N, uint32_t *bits)
 // every group uniform in whether its strings end within h0 symbols: without
 // it a suffix of exactly h0 symbols would tie with longer suffixes sharing
 // those symbols.  The recoding is monotone, so the order is the byte order.
+// Also writes rem8[x] = min(rem(x), 255) (see DictRem).
 __global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, const uint8_t *code, int bps, int h0,
-                            uint64_t *keys)
+                            uint64_t *keys, uint8_t *rem8)
 {
     __shared__ uint8_t s_code[256];
     s_code[threadIdx.x] = code[threadIdx.x];     // blockDim == 256
@@ -812,6 +822,7 @@ __global__ void k_dict_keys(const uint8_t *dict, uint32_t N, DictRem rem, const 
     for (int i = 0; i < h0; i++) key = (key << bps) | (uint64_t)((uint32_t)i < r ? s_code[dict[x + i]] : 0u);
     key = (key << 1) | (r > (uint32_t)h0 ? 1u : 0u);
     keys[x] = key;
+    rem8[x] = (uint8_t)(r < 255u ? r : 255u);
 }
 
 // Dense lexicographic rank of each distinct phrase.  After the sort, isa[x]
@@ -851,7 +862,7 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
     (void)W;
     (void)small;   // the alphabet recoding below covers the small-alphabet packing
     const uint32_t N = (uint32_t)ph.dict_bytes;
-    DictRem rem{ph.dphr, ph.doff, ph.dlen};
+    DictRem rem{ph.dphr, ph.doff, ph.dlen, nullptr};
     // alphabet of the dictionary -> dense codes 1..sigma
     check_cuda(cudaMemsetAsync(st->d_flags + 8, 0, 8 * sizeof(uint32_t), st->stream));
     unsigned ag = grid_for(N, 256);
@@ -877,8 +888,10 @@ void run_dict_sort(Storage *st, Phrases &ph, int W, bool small, DictOrder &dord)
     uint8_t *dcode = slot<uint8_t>(st, S_TMP1, 256);
     check_cuda(cudaMemcpyAsync(dcode, hcode, 256, cudaMemcpyHostToDevice, st->stream));
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, N);
-    k_dict_keys<<<grid_for(N, 256), 256, 0, st->stream>>>(ph.dict, N, rem, dcode, bps, h0, keys);
+    uint8_t *rem8 = slot<uint8_t>(st, S_TMP0, N);
+    k_dict_keys<<<grid_for(N, 256), 256, 0, st->stream>>>(ph.dict, N, rem, dcode, bps, h0, keys, rem8);
     after_launch(st);
+    rem.rem8 = rem8;
     dord.isa = slot<uint32_t>(st, S_ISA, N);
     dord.sa = slot<uint32_t>(st, S_SA, N);
     dord.rounds = prefix_doubling(st, N, h0 * bps + 1, (uint32_t)h0, rem, dord.isa, dord.sa, true);
