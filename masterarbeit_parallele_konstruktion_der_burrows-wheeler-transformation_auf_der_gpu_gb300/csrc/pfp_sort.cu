@@ -480,9 +480,15 @@ __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, con
         gnew = a == 0 || act_g[a - 1] != g;
         if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
     }
-    // a warp's 32 indices lie in one tile (blockDim and SS_TILE multiples of 32)
+    // a block's indices lie in one tile (blockDim divides SS_TILE): one
+    // global atomic per block with a group start
+    __shared__ uint32_t s_first;
+    if (threadIdx.x == 0) s_first = 0xFFFFFFFFu;
+    __syncthreads();
     const uint32_t first = __reduce_min_sync(0xFFFFFFFFu, gnew ? a : 0xFFFFFFFFu);
-    if ((threadIdx.x & 31u) == 0 && first != 0xFFFFFFFFu) atomicMin(tstart + first / SS_TILE, first);
+    if ((threadIdx.x & 31u) == 0 && first != 0xFFFFFFFFu) atomicMin(&s_first, first);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_first != 0xFFFFFFFFu) atomicMin(tstart + s_first / SS_TILE, s_first);
 }
 
 template <typename Rem>
@@ -726,6 +732,7 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles);
         check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
         check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4, st->stream));
+        static_assert(SS_TILE % 256 == 0, "gather blocks must not straddle tiles");
         k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
                                                                  st->d_flags, tstart);
         after_launch(st);
