@@ -466,9 +466,9 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
 }
 
 // key2[a] = isa[x+h] + 1 for every active element (all reads of this round's
-// ranks happen before any update); flags[3] counts groups too large for the
-// shared-memory path; tstart[b] = first group start in tile b (SS_TILE
-// active indices; 0xFFFFFFFF before, via memset).
+// ranks happen before any update); with flags, flags[3] counts groups too
+// large for the shared-memory path; tstart[b] = first group start in tile b
+// (SS_TILE active indices; 0xFFFFFFFF before, via memset).
 __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
                                uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart)
 {
@@ -478,7 +478,7 @@ __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, con
         key2[a] = isa[act_x[a] + h] + 1u;
         const uint32_t g = act_g[a];
         gnew = a == 0 || act_g[a - 1] != g;
-        if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
+        if (flags && gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
     }
     // a block's indices lie in one tile (blockDim divides SS_TILE): one
     // global atomic per block with a group start
@@ -723,6 +723,10 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         ss_attr = true;
     }
     const bool debug = getenv("GBWT_DEBUG") != nullptr;
+    // groups only split, so after a segmented round no group exceeds
+    // SS_SEGMAX: the size check (and its host round trip) is needed only
+    // after round 0 and after global rounds
+    bool check_big = true;
     while (A > 0) {
         if (h >= N) throw Error{GBWT_INTERNAL_ERROR};
         const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
@@ -730,15 +734,19 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
         uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
         const uint32_t ss_tiles = grid_for(A, SS_TILE);
         uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles);
-        check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
+        if (check_big) check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
         check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4, st->stream));
         static_assert(SS_TILE % 256 == 0, "gather blocks must not straddle tiles");
         k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
-                                                                 st->d_flags, tstart);
+                                                                 check_big ? st->d_flags : nullptr, tstart);
         after_launch(st);
-        check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
-        check_cuda(cudaStreamSynchronize(st->stream));
-        const bool big = ((uint32_t)st->h_scalars[2]) != 0;      // a group above SS_SEGMAX
+        bool big = false;                                         // a group above SS_SEGMAX
+        if (check_big) {
+            check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
+            check_cuda(cudaStreamSynchronize(st->stream));
+            big = ((uint32_t)st->h_scalars[2]) != 0;
+        }
+        check_big = big;
         if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u path=%s\n", (unsigned long long)h, A,
                            big ? "global" : "segmented");
         if (!big) {
