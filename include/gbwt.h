@@ -103,7 +103,9 @@ int64_t gbwt_set_stream(void *storage, void *cuda_stream);
  * PFP BWT of one text: T[0..n) -> L[0..n).  Replaces the process-level
  * pipeline of the reference's main() (K:4793-4815: Compute_D K:2415-2506,
  * then Compute_S K:4330-4771) for one (W, P, small_alphabet) variant
- * (Makefile:11-23).  W in [1,64], P in [2,65535].  Returns n on success.
+ * (Makefile:11-23).  W in [1,64], P in [1,65535] (every entry point
+ * accepts the same range; P = 1 makes every window after the first a
+ * trigger, since every hash is 0 mod 1).  Returns n on success.
  */
 int64_t gbwt_pfp_bwt(void *storage, const uint8_t *T, uint8_t *L, int64_t n,
                      int32_t W, int32_t P, uint32_t flags);
@@ -124,7 +126,9 @@ int64_t gbwt_pfp_bwt_batch(void *storage, const uint8_t *T_concat, const int64_t
 /*
  * Trigger scan only: writes the phrase end positions D[0..z) (the last is
  * n+W-1) and returns z.  Replaces Compute_D1/D2/D3 (K:443-576, driver
- * K:2415-2455).  Returns GBWT_BAD_PARAMETER when capacity < z.
+ * K:2415-2455).  Returns GBWT_BAD_PARAMETER when capacity < z.  Only the
+ * windows starting at 1..n-W can trigger, plus the forced final trigger, so
+ * z <= max(n - W + 1, 1) and capacity = n + 1 always suffices.
  */
 int64_t gbwt_pfp_trigger_scan(void *storage, const uint8_t *T, int64_t n, int32_t W,
                               int32_t P, uint32_t flags, int64_t *D, int64_t capacity);
@@ -148,13 +152,18 @@ int64_t gbwt_pfp_parse(void *storage, const uint8_t *T, int64_t n, int32_t W, in
  * process that reserved all device memory up front).  T (n bytes) and D
  * (capacity uint32 slots) are DEVICE pointers owned by the caller; `stream`
  * is a cudaStream_t (NULL = legacy default stream).  Writes the phrase end
- * positions D[0..z) exactly like gbwt_pfp_trigger_scan and returns z after
- * synchronising the stream.
+ * positions D[0..z) exactly like gbwt_pfp_trigger_scan and returns z.
+ * Capacity: z <= max(n - W + 1, 1), so capacity = n + 1 always suffices;
+ * a smaller capacity that turns out too small gives GBWT_BAD_PARAMETER.
  * Limits: n <= 2^30 bytes.  The scratch is one library-wide device array of
  * about 1 MiB that every GPU loading the library keeps until exit; the first
- * call on a device looks up its address (do that call before any stream
- * capture).  Calls that overlap on the GPU race on that array and must be
- * serialised by the caller; each call clears what must start at zero.
+ * call on a device checks that the device is an sm_103 GPU
+ * (GBWT_GPU_NOT_SUPPORTED otherwise, before any device work) and looks up
+ * the array's address.  Every call reads the trigger count back between its
+ * two passes and synchronises `stream` before it returns, so it must not be
+ * called on a stream that is being captured into a CUDA graph.  Calls that
+ * overlap on the GPU race on the shared array and must be serialised by the
+ * caller; each call clears what must start at zero.
  */
 int64_t gbwt_pfp_trigger_scan_noalloc(const uint8_t *T, int64_t n, int32_t W, int32_t P, uint32_t flags,
                                       uint32_t *D, int64_t capacity, void *stream);

@@ -569,6 +569,9 @@ static __device__ __align__(256) uint32_t g_trigger_scratch[NOALLOC_SCRATCH_WORD
 
 // Device address of g_trigger_scratch for the current device, looked up
 // once per device (the host-side symbol itself is not a device address).
+// The same first call checks the compute capability, so an unsupported GPU
+// gets GBWT_GPU_NOT_SUPPORTED before any work is queued on the caller's
+// stream (the kernels are built for sm_103a only).
 static uint32_t *noalloc_scratch_ptr()
 {
     static uint32_t *ptrs[64] = {};
@@ -578,6 +581,10 @@ static uint32_t *noalloc_scratch_ptr()
     if (dev < 0 || dev >= 64) throw Error{GBWT_GPU_NOT_SUPPORTED};
     std::lock_guard<std::mutex> lock(mu);
     if (!ptrs[dev]) {
+        int major = 0, minor = 0;
+        check_cuda(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+        check_cuda(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+        if (major * 10 + minor != 103) throw Error{GBWT_GPU_NOT_SUPPORTED};
         void *p = nullptr;
         check_cuda(cudaGetSymbolAddress(&p, g_trigger_scratch));
         ptrs[dev] = (uint32_t *)p;

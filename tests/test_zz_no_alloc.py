@@ -51,6 +51,30 @@ def test_noalloc_matches_storage_entry_point(pkg, wl, W, P, small):
         assert np.array_equal(got, want), call
 
 
+@pytest.mark.parametrize("n", [20 * (1 << 20) + 12345, 32 * (1 << 20)])
+def test_noalloc_large_text_matches_oracle(pkg, wl, orc, n):
+    # more than 4096 CTAs of 4 KiB: the per-CTA counts are scanned in several tiles
+    # (reduce, scan of the tile partials, down-sweep); 32 MiB is an exact multiple of
+    # one scan tile's 16 MiB.  Compared with the oracle's trigger scan directly.
+    torch = pytest.importorskip("torch")
+    fn = _fn(pkg)
+    base = wl.config1_text()
+    text = np.resize(base, n).astype(np.uint8)
+    text[::7919] = 5                                  # the copies are not identical
+    want = orc.trigger_scan(text, 5, 16)
+    dT = torch.from_numpy(text).cuda()
+    cap = n + 1                                       # z <= n - W + 1 always fits
+    dD = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    torch.cuda.synchronize()
+    for call in range(2):
+        dD.fill_(-1)
+        torch.cuda.synchronize()
+        z = fn(dT.data_ptr(), n, 5, 16, 0, dD.data_ptr(), cap, stream)
+        assert z == len(want), (call, z, len(want))
+        assert np.array_equal(dD[:z].cpu().numpy().astype(np.int64), want), call
+
+
 def test_noalloc_limits_and_errors(pkg):
     torch = pytest.importorskip("torch")
     fn = _fn(pkg)
