@@ -199,18 +199,61 @@ def run_pfp(text, W: int, P: int, small: bool, timeout: float = 600.0, checked: 
     t = np.ascontiguousarray(text, dtype=np.uint8)
     d = _tmpdir()
     try:
-        tin, tout = os.path.join(d, "text.bin"), os.path.join(d, "bwt.bin")
+        tin = os.path.join(d, "text.bin")
         t.tofile(tin)
-        r = subprocess.run([pfp_binary(variant), tin, tout], capture_output=True, text=True, timeout=timeout)
-        if r.returncode != 0:
-            raise RuntimeError(f"reference {variant} exited {r.returncode}: {r.stderr[-1000:]}")
-        info = json.loads(r.stdout.strip().splitlines()[-1])
-        L = np.fromfile(tout, dtype=np.uint8)
+        return _run_pfp_file(variant, tin, len(t), d, timeout, keep_output=True)
     finally:
         shutil.rmtree(d, ignore_errors=True)
-    if len(L) != len(t):
-        raise RuntimeError(f"reference {variant} wrote {len(L)} bytes for a {len(t)}-byte text")
+
+
+def _run_pfp_file(variant: str, text_path: str, n: int, workdir: str, timeout: float, keep_output: bool):
+    out = os.path.join(workdir, "bwt.bin")
+    r = subprocess.run([pfp_binary(variant), text_path, out], capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference {variant} exited {r.returncode}: {r.stderr[-1000:]}")
+    info = json.loads(r.stdout.strip().splitlines()[-1])
+    L = np.fromfile(out, dtype=np.uint8) if keep_output else None
+    os.remove(out)
+    if keep_output and len(L) != n:
+        raise RuntimeError(f"reference {variant} wrote {len(L)} bytes for a {n}-byte text")
     return L, info
+
+
+class PfpSession:
+    """Repeated runs of one reference PFP program on one text, written to a file once.
+
+    The guard runs once in the constructor (ReferenceRefused without a
+    launch); each ``run()`` is one process run of the program: one BWT,
+    returned with its times when ``keep_output``.
+    """
+
+    def __init__(self, text, W: int, P: int, small: bool, timeout: float = 600.0):
+        self.variant = variant_name(W, P, small)
+        if self.variant not in PFP_VARIANTS:
+            raise ValueError(f"the reference has no program for {self.variant}")
+        if not available(self.variant):
+            raise FileNotFoundError(pfp_binary(self.variant))
+        why = guard(text, W, P, small)
+        if why is not None:
+            raise ReferenceRefused(why)
+        t = np.ascontiguousarray(text, dtype=np.uint8)
+        self.n = len(t)
+        self.timeout = timeout
+        self.dir = _tmpdir()
+        self.path = os.path.join(self.dir, "text.bin")
+        t.tofile(self.path)
+
+    def run(self, keep_output: bool = False):
+        return _run_pfp_file(self.variant, self.path, self.n, self.dir, self.timeout, keep_output)
+
+    def close(self):
+        shutil.rmtree(self.dir, ignore_errors=True)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def run_libcubwt(text, repetitions: int = 1, timeout: float = 600.0):
