@@ -225,7 +225,10 @@ typedef struct gbwt_tuning {
     int32_t unbwt_rate_log2;    /* inverse BWT: one ruler per 2^k rows (2..12; default 7)            */
     int32_t dict_key_bits;      /* dictionary sort, first key: at most this many bits of recoded
                                    symbols (8..64; default 64: as many symbols as fit)             */
-    int32_t parse_key_phrases;  /* parse suffix array, first key: 1 or 2 phrase ranks (default 2)  */
+    int32_t parse_key_phrases;  /* parse suffix array, first round: 1 or 2 phrase ranks sorted by
+                                   radix; 0 (default): one text's first round comes straight from
+                                   the phrase buckets of the dictionary order, no sort (batches
+                                   then sort 2 ranks)                                              */
     int32_t mixed_radix_bits;   /* mixed-block element sort digit width: 8 or 10 (default 8)       */
     int32_t batch_ballot;       /* batch output sort ranking: every k-th item by ballots (2 or 3),
                                    1 = match only (default 3)                                       */

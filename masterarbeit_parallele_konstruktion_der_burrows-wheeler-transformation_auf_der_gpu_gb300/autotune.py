@@ -30,7 +30,7 @@ PKG = os.path.basename(os.path.dirname(os.path.abspath(__file__)))
 CANDIDATES = {
     "hash_log2_max": (20, 22, 24),
     "dict_key_bits": (64, 48, 40, 32),
-    "parse_key_phrases": (1, 2),
+    "parse_key_phrases": (0, 1, 2),
     "mixed_radix_bits": (8, 10),
     "batch_seg_tiles": (4, 8, 16, 32),
     "batch_pad_eighths": (1, 2, 4),
@@ -40,7 +40,7 @@ CANDIDATES = {
 }
 TEXT_KNOBS = ("hash_log2_max", "dict_key_bits", "parse_key_phrases", "mixed_radix_bits")
 BATCH_KNOBS = ("batch_seg_tiles", "batch_pad_eighths", "batch_radix_bits", "batch_ballot")
-START = {"hash_log2_max": 22, "dict_key_bits": 64, "parse_key_phrases": 2, "mixed_radix_bits": 8, "batch_seg_tiles": 8,
+START = {"hash_log2_max": 22, "dict_key_bits": 64, "parse_key_phrases": 0, "mixed_radix_bits": 8, "batch_seg_tiles": 8,
          "batch_pad_eighths": 1, "batch_radix_bits": 0, "batch_ballot": 3, "unbwt_rate_log2": 7}
 
 

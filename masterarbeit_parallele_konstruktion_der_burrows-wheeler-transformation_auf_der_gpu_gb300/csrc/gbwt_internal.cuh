@@ -33,6 +33,7 @@ enum Slot : int {
     S_SCAN0, S_SCAN1, S_SCAN2, S_SCAN3, S_RSHIST,
     S_TMP0, S_TMP1, S_TMP2, S_PIDPC, S_TILEG, S_ACTX2, S_ACTG2, S_LCB, S_LCBMAP,
     S_BX, S_BMETA, S_BTID, S_BZEND, S_BLAST, S_BCODE, S_SSTART,
+    S_BIGL, S_BIGM,
     S_NUM
 };
 
@@ -143,10 +144,10 @@ inline int tune_seg_tiles(const Storage *st) { return st->tuning.batch_seg_tiles
 inline int tune_pad_eighths(const Storage *st) { return st->tuning.batch_pad_eighths ? st->tuning.batch_pad_eighths : 1; }
 inline int tune_unbwt_rate_log2(const Storage *st) { return st->tuning.unbwt_rate_log2 ? st->tuning.unbwt_rate_log2 : 7; }
 inline int tune_dict_key_bits(const Storage *st) { return st->tuning.dict_key_bits ? st->tuning.dict_key_bits : 64; }
-inline int tune_parse_key_phrases(const Storage *st)
-{
-    return st->tuning.parse_key_phrases ? st->tuning.parse_key_phrases : 2;
-}
+// 0 (default): single-text parse round 0 from the phrase buckets, no sort
+// (the batch parse then sorts two phrase ranks); 1 or 2: a radix sort of
+// the first one or two phrase ranks.
+inline int tune_parse_key_phrases(const Storage *st) { return st->tuning.parse_key_phrases; }
 
 inline int bits_for(uint64_t v)   // bits needed to represent values in [0, v]
 {

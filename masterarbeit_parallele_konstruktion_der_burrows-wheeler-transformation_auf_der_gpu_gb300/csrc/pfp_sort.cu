@@ -24,6 +24,8 @@
 #include "prims.cuh"
 #include <stdio.h>
 #include <stdlib.h>
+#include <algorithm>
+#include <vector>
 
 namespace gbwt {
 
@@ -466,11 +468,17 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
 }
 
 // key2[a] = isa[x+h] + 1 for every active element (all reads of this round's
-// ranks happen before any update); with flags, flags[3] counts groups too
-// large for the shared-memory path; tstart[b] = first group start in tile b
-// (SS_TILE active indices; 0xFFFFFFFF before, via memset).
+// ranks happen before any update); tstart[b] = first group start in tile b
+// (SS_TILE active indices; 0xFFFFFFFF before, via memset).  With `bigs`,
+// groups too large for the shared-memory path (more than SS_SEGMAX members)
+// are listed: flags[3] / flags[4] count their starts / ends, bigs[i] = the
+// i-th start, bigs[big_cap + i] = the i-th end (one past the last member;
+// both lists in no particular order), and tbig[b] = the start of the one that
+// starts in tile b (a tile holds at most one: such a group is longer than a
+// tile).
 __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
-                               uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart)
+                               uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart, uint32_t *bigs,
+                               uint32_t big_cap, uint32_t *tbig)
 {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     bool gnew = false;
@@ -478,7 +486,20 @@ __global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, con
         key2[a] = isa[act_x[a] + h] + 1u;
         const uint32_t g = act_g[a];
         gnew = a == 0 || act_g[a - 1] != g;
-        if (flags && gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) atomicAdd(flags + 3, 1u);
+        if (bigs) {
+            if (gnew && a + SS_SEGMAX < A && act_g[a + SS_SEGMAX] == g) {
+                const uint32_t i = atomicAdd(flags + 3, 1u);
+                if (i < big_cap) bigs[i] = a;
+                else atomicOr(flags, ERR_INTERNAL);
+                tbig[a / SS_TILE] = a;
+            }
+            const bool gend = a + 1u == A || act_g[a + 1u] != g;
+            if (gend && a >= SS_SEGMAX && act_g[a - SS_SEGMAX] == g) {
+                const uint32_t i = atomicAdd(flags + 4, 1u);
+                if (i < big_cap) bigs[big_cap + i] = a + 1u;
+                else atomicOr(flags, ERR_INTERNAL);
+            }
+        }
     }
     // a block's indices lie in one tile (blockDim divides SS_TILE): one
     // global atomic per block with a group start
@@ -495,7 +516,8 @@ template <typename Rem>
 __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__restrict__ act_x,
                                                             const uint32_t *__restrict__ act_g,
                                                             const uint32_t *__restrict__ key2,
-                                                            const uint32_t *__restrict__ tstart, uint32_t A,
+                                                            const uint32_t *__restrict__ tstart,
+                                                            const uint32_t *__restrict__ tbig, uint32_t A,
                                                             uint32_t h2, Rem rem, uint32_t *isa, uint32_t *sa,
                                                             uint32_t *out_x, uint32_t *out_g, uint32_t *counter,
                                                             uint32_t *flags, bool collect_stats)
@@ -517,13 +539,23 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     // first group start in the next tile (or A)
     const uint32_t s0 = tstart[blockIdx.x];
     if (s0 == 0xFFFFFFFFu) return;                   // no group starts in this tile
-    uint32_t e1 = blockIdx.x + 1 < gridDim.x ? tstart[blockIdx.x + 1] : A;
-    if (e1 == 0xFFFFFFFFu) {
-        // only the last tile, partly filled, may lack a start
-        if (blockIdx.x + 2 < gridDim.x) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
-        e1 = A;
+    uint32_t e1;
+    const uint32_t bstart = tbig ? tbig[blockIdx.x] : 0xFFFFFFFFu;
+    if (bstart != 0xFFFFFFFFu) {
+        // a group too large for this path starts in this tile (at or after
+        // s0) and runs past it: the range ends there, the big-group path
+        // sorts it
+        e1 = bstart;
+    } else {
+        e1 = blockIdx.x + 1 < gridDim.x ? tstart[blockIdx.x + 1] : A;
+        if (e1 == 0xFFFFFFFFu) {
+            // only the last tile, partly filled, may lack a start
+            if (blockIdx.x + 2 < gridDim.x) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
+            e1 = A;
+        }
     }
     const uint32_t cnt = e1 - s0;
+    if (cnt == 0) return;
     if (cnt > (uint32_t)SS_CAP) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
 
     // coalesced loads into shared memory (s_nh holds the group ids for now)
@@ -686,6 +718,188 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
     }
 }
 
+__global__ void k_big_heads(const uint32_t *act_g, const uint32_t *bstart, uint32_t nbig, uint32_t *bhead)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nbig) bhead[i] = act_g[bstart[i]];
+}
+
+// ---------------------------------------------------------------------
+// Big-group path.  Groups with more than SS_SEGMAX members (listed by the
+// gather, cut out of the segmented kernel's ranges) are sorted together by
+// one global radix sort over their members only, keyed (big-group index,
+// isa[x+h] + 1); one scan derives the new heads, one scan appends the
+// members that stay active to the next active list after the ones the
+// segmented kernel wrote.  In a repetitive text only a few groups (frequent
+// short phrases, early rounds) take it.
+// ---------------------------------------------------------------------
+__global__ void k_big_keys(const uint32_t *bstart, const uint32_t *boff, uint32_t nbig, const uint32_t *key2,
+                           const uint32_t *act_x, int lb, uint64_t *keys, uint32_t *vals)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t total = boff[nbig];
+    if (t >= total) return;
+    uint32_t lo = 0, hi = nbig - 1u;                 // last group with boff <= t
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (boff[mid] <= t) lo = mid; else hi = mid - 1u;
+    }
+    const uint32_t a = bstart[lo] + (t - boff[lo]);
+    keys[t] = ((uint64_t)lo << lb) | (uint64_t)key2[a];
+    vals[t] = act_x[a];
+}
+template <typename Rem>
+struct StoreBigRound {
+    ActiveTest<Rem> t;
+    int lb;
+    const uint32_t *bhead;
+    uint32_t *isa;
+    uint32_t *head;
+    uint32_t *sa;
+    __device__ __forceinline__ void operator()(size_t a, uint64_t inc, uint64_t) const
+    {
+        const uint32_t g = bhead[(uint32_t)(t.k[a] >> lb)];
+        const uint32_t ag = (uint32_t)(inc >> 32), s2 = (uint32_t)inc;
+        const uint32_t nh = g + (s2 - ag);
+        const uint32_t x = t.vals[a];
+        if (nh != g) isa[x] = nh;                     // isa[x] holds the old head g
+        head[a] = nh;
+        if (t.done(a)) sa[g + ((uint32_t)a - ag)] = x;
+    }
+};
+template <typename Rem>
+struct StoreBigActive {
+    ActiveTest<Rem> a;
+    const uint32_t *head;
+    const uint32_t *counter;      // elements the segmented kernel appended
+    uint32_t *act_x;
+    uint32_t *act_g;
+    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t v) const
+    {
+        if (v) {
+            const uint32_t base = *counter;
+            act_x[base + pre] = a.vals[t];
+            act_g[base + pre] = head[t];
+        }
+    }
+};
+
+template <typename Rem>
+static void big_groups(Storage *st, uint32_t N, uint32_t nbig, const uint32_t *dbigs, uint32_t big_cap, uint32_t h2,
+                       const uint32_t *key2, const uint32_t *act_x, const uint32_t *act_g, Rem rem, uint32_t *isa,
+                       uint32_t *sa, uint32_t *out_x, uint32_t *out_g)
+{
+    // starts and ends, both sorted: big groups are disjoint ranges, so the
+    // i-th start and the i-th end delimit the i-th group
+    std::vector<uint32_t> hb(nbig), he(nbig), hoff(nbig + 1);
+    check_cuda(cudaMemcpyAsync(hb.data(), dbigs, (size_t)nbig * 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaMemcpyAsync(he.data(), dbigs + big_cap, (size_t)nbig * 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    std::sort(hb.begin(), hb.end());
+    std::sort(he.begin(), he.end());
+    hoff[0] = 0;
+    for (uint32_t i = 0; i < nbig; i++) {
+        if (he[i] <= hb[i] + SS_SEGMAX || (i + 1 < nbig && he[i] > hb[i + 1])) throw Error{GBWT_INTERNAL_ERROR};
+        hoff[i + 1] = hoff[i] + (he[i] - hb[i]);
+    }
+    const uint32_t total = hoff[nbig];
+    uint32_t *meta = slot<uint32_t>(st, S_BIGM, (size_t)nbig * 3 + 2);   // starts, offsets, heads
+    check_cuda(cudaMemcpyAsync(meta, hb.data(), (size_t)nbig * 4, cudaMemcpyHostToDevice, st->stream));
+    check_cuda(cudaMemcpyAsync(meta + nbig, hoff.data(), (size_t)(nbig + 1) * 4, cudaMemcpyHostToDevice,
+                               st->stream));
+    uint32_t *bhead = meta + 2 * nbig + 1;
+    k_big_heads<<<grid_for(nbig, 256), 256, 0, st->stream>>>(act_g, meta, nbig, bhead);
+    after_launch(st);
+    const int lb = bits_for(N);
+    uint64_t *k = slot<uint64_t>(st, S_KEY0, total);
+    uint64_t *k_alt = slot<uint64_t>(st, S_KEY1, total);
+    uint32_t *v = slot<uint32_t>(st, S_VAL0, total);
+    uint32_t *v_alt = slot<uint32_t>(st, S_VAL1, total);
+    uint32_t *head = slot<uint32_t>(st, S_HEAD, total);
+    k_big_keys<<<grid_for(total, 256), 256, 0, st->stream>>>(meta, meta + nbig, nbig, key2, act_x, lb, k, v);
+    after_launch(st);
+    radix_sort<uint64_t, true>(st, k, k_alt, v, v_alt, total, 0, lb + bits_for(nbig - 1u));
+    ActiveTest<Rem> t{k, v, total, h2, rem};
+    device_scan<uint64_t, OpMax2>(st, total, LoadRoundHead{k, lb}, StoreBigRound<Rem>{t, lb, bhead, isa, head, sa},
+                                  true, (uint64_t *)nullptr);
+    check_cuda(cudaMemsetAsync(st->d_scalars + 1, 0, 8, st->stream));
+    device_scan<uint32_t, OpAdd>(st, total, LoadActive<Rem>{t},
+                                 StoreBigActive<Rem>{t, head, (const uint32_t *)st->d_scalars, out_x, out_g}, false,
+                                 (uint32_t *)(st->d_scalars + 1));
+}
+
+// Prefix-doubling rounds from prefix length h with A active elements listed
+// group by group in act_x (suffix) / act_g (group head); isa holds every
+// suffix's group head and sa every finished slot.  Returns the rounds run.
+template <typename Rem>
+static int doubling_rounds(Storage *st, uint32_t N, uint64_t h, uint32_t A, Rem rem, uint32_t *isa, uint32_t *sa,
+                           uint32_t *act_x, uint32_t *act_g, uint32_t *act_x2, uint32_t *act_g2, bool check_big)
+{
+    int rounds = 0;
+    static bool ss_attr = false;
+    if (!ss_attr) {
+        check_cuda(cudaFuncSetAttribute(k_seg_sort<Rem>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SS_SMEM));
+        ss_attr = true;
+    }
+    const bool debug = getenv("GBWT_DEBUG") != nullptr;
+    // groups only split: once a round has no group above SS_SEGMAX, no later
+    // round has one, and the big-group listing (and its host round trip) stops
+    while (A > 0) {
+        if (h >= N) throw Error{GBWT_INTERNAL_ERROR};
+        const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
+        // gather this round's keys before any rank changes; list big groups
+        uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
+        const uint32_t ss_tiles = grid_for(A, SS_TILE);
+        uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles * 2);
+        uint32_t *tbig = tstart + ss_tiles;
+        const uint32_t big_cap = A / SS_SEGMAX + 1u;
+        uint32_t *bigs = check_big ? slot<uint32_t>(st, S_BIGL, (size_t)big_cap * 2) : nullptr;
+        if (check_big) check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 8, st->stream));
+        check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4 * (check_big ? 2 : 1), st->stream));
+        static_assert(SS_TILE % 256 == 0, "gather blocks must not straddle tiles");
+        k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
+                                                                 st->d_flags, tstart, bigs, big_cap, tbig);
+        after_launch(st);
+        uint32_t nbig = 0;
+        if (check_big) {
+            check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 8, cudaMemcpyDeviceToHost, st->stream));
+            check_cuda(cudaStreamSynchronize(st->stream));
+            const uint32_t *cnt = (const uint32_t *)(st->h_scalars + 2);
+            nbig = cnt[0];
+            if (nbig > big_cap || cnt[1] != nbig) throw Error{GBWT_INTERNAL_ERROR};
+        }
+        check_big = nbig > 0;
+        if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u big groups=%u\n", (unsigned long long)h, A, nbig);
+        uint32_t *counter = (uint32_t *)st->d_scalars;
+        check_cuda(cudaMemsetAsync(st->d_scalars, 0, 16, st->stream));
+        if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 8 * sizeof(uint32_t), st->stream));
+        probe_begin(st, GBWT_PROBE_SEG_SORT);
+        k_seg_sort<Rem><<<ss_tiles, SS_THREADS, SS_SMEM, st->stream>>>(
+            act_x, act_g, key2, tstart, nbig ? tbig : nullptr, A, h2, rem, isa, sa, act_x2, act_g2, counter,
+            st->d_flags, debug);
+        // per active element: read x, group, key (12 B); write its rank and
+        // either its next-round (x, group) or its final suffix-array slot (12 B)
+        probe_end(st, GBWT_PROBE_SEG_SORT, 24ull * A);
+        after_launch(st);
+        if (nbig) big_groups<Rem>(st, N, nbig, bigs, big_cap, h2, key2, act_x, act_g, rem, isa, sa, act_x2, act_g2);
+        fetch_scalars(st, 2);
+        if (debug) {
+            uint32_t tiers[8];
+            check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
+            fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
+                    SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
+            fprintf(stderr, "gbwt:   larger groups: one value %u, majority + <=32 outliers %u, other %u\n",
+                    tiers[4], tiers[7], tiers[6]);
+        }
+        A = (uint32_t)st->h_scalars[0] + (uint32_t)st->h_scalars[1];
+        uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
+        uint32_t *t2 = act_g; act_g = act_g2; act_g2 = t2;
+        h *= 2;
+        rounds++;
+    }
+    return rounds;
+}
+
 // Sorts N positions; key0 (in slot S_KEY0) holds the initial keys covering
 // h0 symbols; with key0_cont, bit 0 of every initial key tells whether the
 // suffix is longer than h0 (rem > h0).  Fills isa[N] and sa[N]; returns the
@@ -700,9 +914,8 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
     uint32_t *vals_alt = slot<uint32_t>(st, S_VAL1, N);
     uint32_t *act_x = slot<uint32_t>(st, S_ACTX, N);
     uint32_t *act_g = slot<uint32_t>(st, S_ACTG, N);
-    uint32_t *act_x2 = slot<uint32_t>(st, S_ACTX2, N);   // next active list (segmented rounds)
+    uint32_t *act_x2 = slot<uint32_t>(st, S_ACTX2, N);   // next active list
     uint32_t *act_g2 = slot<uint32_t>(st, S_ACTG2, N);
-    int rounds = 1;
 
     k_iota<<<grid_for(N, 256), 256, 0, st->stream>>>(vals, N);
     after_launch(st);
@@ -713,90 +926,8 @@ static int prefix_doubling(Storage *st, uint32_t N, int key0_bits, uint32_t h0, 
                                     StoreHeadActive0<Rem>{at, isa, sa, act_x, act_g},
                                     false, (uint64_t *)st->d_scalars);
     fetch_scalars(st, 1);
-    uint32_t A = (uint32_t)st->h_scalars[0];      // low word of the total: active elements
-    const int lb = bits_for(N);          // isa+1 <= N
-    const int gb = bits_for(N - 1);
-    uint64_t h = h0;
-    static bool ss_attr = false;
-    if (!ss_attr) {
-        check_cuda(cudaFuncSetAttribute(k_seg_sort<Rem>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SS_SMEM));
-        ss_attr = true;
-    }
-    const bool debug = getenv("GBWT_DEBUG") != nullptr;
-    // groups only split, so after a segmented round no group exceeds
-    // SS_SEGMAX: the size check (and its host round trip) is needed only
-    // after round 0 and after global rounds
-    bool check_big = true;
-    while (A > 0) {
-        if (h >= N) throw Error{GBWT_INTERNAL_ERROR};
-        const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
-        // gather this round's keys before any rank changes; count big groups
-        uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
-        const uint32_t ss_tiles = grid_for(A, SS_TILE);
-        uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles);
-        if (check_big) check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 4, st->stream));
-        check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4, st->stream));
-        static_assert(SS_TILE % 256 == 0, "gather blocks must not straddle tiles");
-        k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
-                                                                 check_big ? st->d_flags : nullptr, tstart);
-        after_launch(st);
-        bool big = false;                                         // a group above SS_SEGMAX
-        if (check_big) {
-            check_cuda(cudaMemcpyAsync(st->h_scalars + 2, st->d_flags + 3, 4, cudaMemcpyDeviceToHost, st->stream));
-            check_cuda(cudaStreamSynchronize(st->stream));
-            big = ((uint32_t)st->h_scalars[2]) != 0;
-        }
-        check_big = big;
-        if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u path=%s\n", (unsigned long long)h, A,
-                           big ? "global" : "segmented");
-        if (!big) {
-            uint32_t *counter = (uint32_t *)st->d_scalars;
-            check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-            if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 8 * sizeof(uint32_t), st->stream));
-            probe_begin(st, GBWT_PROBE_SEG_SORT);
-            k_seg_sort<Rem><<<ss_tiles, SS_THREADS, SS_SMEM, st->stream>>>(
-                act_x, act_g, key2, tstart, A, h2, rem, isa, sa, act_x2, act_g2, counter, st->d_flags, debug);
-            // per active element: read x, group, key (12 B); write its rank and
-            // either its next-round (x, group) or its final suffix-array slot (12 B)
-            probe_end(st, GBWT_PROBE_SEG_SORT, 24ull * A);
-            after_launch(st);
-            fetch_scalars(st, 1);
-            if (debug) {
-                uint32_t tiers[8];
-                check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
-                fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
-                        SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
-                fprintf(stderr, "gbwt:   larger groups: one value %u, majority + <=32 outliers %u, other %u\n",
-                        tiers[4], tiers[7], tiers[6]);
-            }
-            A = (uint32_t)st->h_scalars[0];
-            uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
-            uint32_t *t2 = act_g; act_g = act_g2; act_g2 = t2;
-            h *= 2;
-            rounds++;
-            continue;
-        }
-        // the key arrays of the previous round are dead: rebuild in place
-        uint32_t *head = slot<uint32_t>(st, S_HEAD, N);
-        uint64_t *k = slot<uint64_t>(st, S_KEY0, N);
-        uint64_t *k_alt = slot<uint64_t>(st, S_KEY1, N);
-        uint32_t *v = slot<uint32_t>(st, S_VAL0, N);
-        uint32_t *v_alt = slot<uint32_t>(st, S_VAL1, N);
-        k_round_keys<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, lb, k, v);
-        after_launch(st);
-        radix_sort<uint64_t, true>(st, k, k_alt, v, v_alt, A, 0, lb + gb);
-        ActiveTest<Rem> t{k, v, A, (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull), rem};
-        device_scan<uint64_t, OpMax2>(st, A, LoadRoundHead{k, lb}, StoreRound<Rem>{t, lb, isa, head, sa}, true,
-                                      (uint64_t *)nullptr);
-        check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
-        device_scan<uint32_t, OpAdd>(st, A, LoadActive<Rem>{t}, StoreActiveR<Rem>{t, head, act_x, act_g}, false,
-                                     (uint32_t *)st->d_scalars);
-        fetch_scalars(st, 1);
-        A = (uint32_t)st->h_scalars[0];
-        h *= 2;
-        rounds++;
-    }
-    return rounds;
+    const uint32_t A = (uint32_t)st->h_scalars[0];      // low word of the total: active elements
+    return 1 + doubling_rounds(st, N, h0, A, rem, isa, sa, act_x, act_g, act_x2, act_g2, true);
 }
 
 // Byte values present in the dictionary (= the text's alphabet plus the
@@ -936,18 +1067,98 @@ __global__ void k_parse_keys(const uint32_t *pid, const uint32_t *lexrank, uint3
     keys[i] = (a << lb) | b;
 }
 
+// Parse round 0 without a sort.  The parse suffix array lists the
+// occurrences of each phrase contiguously, phrases in lexicographic order, so
+// the first-round group of an occurrence is its phrase's bucket, which starts
+// at the number of occurrences of all lower-ranked phrases.  Every
+// occurrence's rank is written in place (coalesced); occurrences of phrases
+// that occur once are finished; the others go to the active list bucket by
+// bucket, in no particular order inside a bucket: the rounds sort every
+// group by its next key and all parse suffixes differ, so no order among
+// equal keys survives to the result.
+__global__ void k_bucket_counts(const uint32_t *lexrank, const uint32_t *occ, uint32_t d, uint32_t *cnt_r)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < d) cnt_r[lexrank[q]] = occ[q];
+}
+// packed per rank: (occurrences << 32) | (occurrences staying active)
+struct LoadBucket {
+    const uint32_t *cnt;
+    __device__ __forceinline__ uint64_t operator()(size_t r) const
+    {
+        const uint32_t c = cnt[r];
+        return ((uint64_t)c << 32) | (c > 1u ? c : 0u);
+    }
+};
+struct StoreBucket {
+    uint64_t *bst;
+    __device__ __forceinline__ void operator()(size_t r, uint64_t pre, uint64_t) const { bst[r] = pre; }
+};
+__global__ void k_bucket_scatter(const uint32_t *pid, const uint32_t *lexrank, const uint64_t *bst,
+                                 const uint32_t *occ, uint32_t z, uint32_t *cur, uint32_t *isa, uint32_t *sa,
+                                 uint32_t *act_x, uint32_t *act_g, uint32_t *flags)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= z) return;
+    const uint32_t q = pid[i];
+    const uint32_t r = lexrank[q];
+    const uint64_t p = bst[r];
+    const uint32_t b = (uint32_t)(p >> 32);
+    isa[i] = b;
+    if (occ[q] == 1u) {
+        if (b < z) sa[b] = i;         // the only suffix starting with this phrase
+        else atomicOr(flags, ERR_INTERNAL);
+    } else {
+        const uint32_t k = atomicAdd(cur + r, 1u);
+        const uint32_t pos = (uint32_t)p + k;
+        if (k < occ[q] && pos < z) {
+            act_x[pos] = i;
+            act_g[pos] = b;
+        } else {
+            atomicOr(flags, ERR_INTERNAL);
+        }
+    }
+}
+
 void run_parse_sa(Storage *st, Phrases &ph, DictOrder &dord, ParseOrder &pord)
 {
     const uint32_t z = ph.z;
-    uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
-    const int lb = bits_for(ph.d);       // lexrank+1 <= d
-    const bool two = tune_parse_key_phrases(st) == 2;
-    k_parse_keys<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, z, lb, two, keys);
-    after_launch(st);
     pord.isa = slot<uint32_t>(st, S_PISA, z);
     pord.sa = slot<uint32_t>(st, S_PSA, z);
-    pord.rounds = prefix_doubling(st, z, two ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), two ? 2u : 1u,
-                                  ParseRem{z}, pord.isa, pord.sa);
+    const int kp = tune_parse_key_phrases(st);
+    if (kp == 1 || kp == 2) {
+        // round 0 by a radix sort of the first one or two phrase ranks
+        uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
+        const int lb = bits_for(ph.d);       // lexrank+1 <= d
+        k_parse_keys<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, z, lb, kp == 2, keys);
+        after_launch(st);
+        pord.rounds = prefix_doubling(st, z, kp == 2 ? lb + bits_for(ph.d - 1) : bits_for(ph.d - 1), (uint32_t)kp,
+                                      ParseRem{z}, pord.isa, pord.sa);
+        return;
+    }
+    // round 0 from the phrase buckets (the last phrase occurs once: its
+    // suffix, the only one ending within one phrase, is finished here)
+    const uint32_t d = ph.d;
+    uint32_t *cnt_r = slot<uint32_t>(st, S_TMP0, d);
+    uint64_t *bst = slot<uint64_t>(st, S_KEY1, d);
+    uint32_t *cur = slot<uint32_t>(st, S_TMP1, d);
+    uint32_t *act_x = slot<uint32_t>(st, S_ACTX, z);
+    uint32_t *act_g = slot<uint32_t>(st, S_ACTG, z);
+    uint32_t *act_x2 = slot<uint32_t>(st, S_ACTX2, z);
+    uint32_t *act_g2 = slot<uint32_t>(st, S_ACTG2, z);
+    k_bucket_counts<<<grid_for(d, 256), 256, 0, st->stream>>>(dord.lexrank, ph.occ, d, cnt_r);
+    after_launch(st);
+    check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
+    device_scan<uint64_t, OpAdd>(st, d, LoadBucket{cnt_r}, StoreBucket{bst}, false, (uint64_t *)st->d_scalars);
+    check_cuda(cudaMemsetAsync(cur, 0, (size_t)d * 4, st->stream));
+    k_bucket_scatter<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bst, ph.occ, z, cur, pord.isa,
+                                                               pord.sa, act_x, act_g, st->d_flags);
+    after_launch(st);
+    fetch_scalars(st, 1);
+    const uint64_t tot = st->h_scalars[0];
+    if ((uint32_t)(tot >> 32) != z) throw Error{GBWT_INTERNAL_ERROR};
+    pord.rounds = 1 + doubling_rounds(st, z, 1, (uint32_t)tot, ParseRem{z}, pord.isa, pord.sa, act_x, act_g, act_x2,
+                                      act_g2, true);
 }
 
 // Batch: the second symbol of a key is 0 when phrase i ends its text.
@@ -970,7 +1181,7 @@ void run_parse_sa_batch(Storage *st, Phrases &ph, DictOrder &dord, const BatchTe
     const uint32_t z = ph.z;
     uint64_t *keys = slot<uint64_t>(st, S_KEY0, z);
     const int lb = bits_for(ph.d);
-    const bool two = tune_parse_key_phrases(st) == 2;
+    const bool two = tune_parse_key_phrases(st) != 1;
     k_parse_keys_batch<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bt.ptid, z, lb, two, keys);
     after_launch(st);
     uint32_t *remv = slot<uint32_t>(st, S_TMP0, z);

@@ -8,9 +8,9 @@ this package; the product path never does.
 Parity anchor: the reference ships no golden vectors; its only correctness
 check compares the PFP output byte for byte with libcubwt's
 (compare_script.sh:7-10).  This restatement is checked against the
-suffix-array BWT in that output convention on every test input; it is not
-pinned against outputs of the reference binaries, which are CUDA programs
-that could not run where the oracle was written.
+suffix-array BWT in that output convention on every test input, and the
+reference's own CUDA programs and its libcubwt copy, built and run by
+``oracle.reference``, are compared with the GPU path on the benchmark texts.
 """
 from __future__ import annotations
 
