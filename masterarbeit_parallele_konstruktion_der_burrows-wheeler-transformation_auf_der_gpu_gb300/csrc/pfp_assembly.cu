@@ -306,60 +306,60 @@ __global__ void k_mixed_scatter(const E *elem, uint32_t M, const uint32_t *delta
     }
 }
 
-// Run fill: 4096 output bytes per CTA, 16 per thread (one 16-byte store);
-// bytes of mixed groups are written as 0 and overwritten by the scatter.
-constexpr int RF_THREADS = 256;
-constexpr int RF_TILE = RF_THREADS * 16;
+// Run fill, one thread per group: the block [goff[g], goff[g+1]) of a run
+// group is one byte repeated; the thread writes the bytes up to the first
+// 16-byte boundary one by one, the middle with 16-byte stores and the tail
+// one by one (neighbouring threads' edge bytes meet in L2).  Mixed groups are
+// skipped: the mixed scatter writes every byte of theirs.  Blocks longer than
+// RF_LONG bytes are listed and filled by one CTA each, so no thread carries a
+// long block.
+constexpr uint32_t RF_LONG = 512;
 
-// tile_first[t] = the group containing output position t*RF_TILE.
-__global__ void k_tile_first(const uint32_t *goff, uint32_t G, uint32_t *tile_first)
+__device__ __forceinline__ void fill_run(uint8_t *out, uint32_t b0, uint32_t b1, uint8_t c)
 {
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= G) return;
-    const uint32_t t0 = (goff[g] + RF_TILE - 1) / RF_TILE, t1 = (goff[g + 1] + RF_TILE - 1) / RF_TILE;
-    for (uint32_t t = t0; t < t1; t++) tile_first[t] = g;
+    uint32_t p = b0;
+    while (p < b1 && (((uintptr_t)(out + p)) & 15u)) out[p++] = c;
+    const uint32_t w = (uint32_t)c * 0x01010101u;
+    const uint4 v = make_uint4(w, w, w, w);
+    for (; p + 16u <= b1; p += 16u) *(uint4 *)(out + p) = v;
+    for (; p < b1; p++) out[p] = c;
 }
 
-__global__ void __launch_bounds__(RF_THREADS) k_run_fill(uint8_t *out, uint32_t n, const uint32_t *goff, uint32_t G,
-                                                         const uint16_t *gchar, const uint8_t *gmix,
-                                                         const uint32_t *tile_first)
+__global__ void k_run_fill_groups(uint8_t *out, uint32_t n, const uint32_t *goff, uint32_t G, const uint16_t *gchar,
+                                  const uint8_t *gmix, uint32_t *longs, uint32_t long_cap, uint32_t *flags)
 {
-    __shared__ uint32_t s_off[RF_TILE + 3];
-    __shared__ uint8_t s_chr[RF_TILE + 3];
-    const uint32_t base = blockIdx.x * RF_TILE;
-    const uint32_t tile_end = min(base + RF_TILE, n);    // exclusive
-    // groups glo .. glo+m-1 cover the tile: from the group containing its first
-    // byte to the one containing tile_end (one group too many when that one
-    // starts exactly at tile_end; it is never selected), m <= RF_TILE + 1
-    const uint32_t glo = tile_first[blockIdx.x];
-    const uint32_t ghi = tile_end < n ? tile_first[blockIdx.x + 1] : G - 1u;
-    const uint32_t m = ghi - glo + 1u;
-    for (uint32_t i = threadIdx.x; i <= m; i += RF_THREADS) {
-        s_off[i] = goff[glo + i];      // goff[G] == n exists
-        if (i < m) s_chr[i] = gmix[glo + i] ? 0 : (uint8_t)gchar[glo + i];
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G || gmix[g]) return;
+    const uint32_t b0 = goff[g], b1 = goff[g + 1];
+    if (b1 < b0 || b1 > n) { atomicOr(flags, ERR_INTERNAL); return; }
+    if (b1 - b0 > RF_LONG) {
+        const uint32_t i = atomicAdd(flags + 5, 1u);
+        if (i < long_cap) longs[i] = g;
+        else atomicOr(flags, ERR_INTERNAL);
+        return;
     }
-    __syncthreads();
-    const uint32_t p0 = base + threadIdx.x * 16u;
-    if (p0 >= tile_end) return;
-    uint32_t lo = 0, hi = m - 1u;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1u) >> 1;
-        if (s_off[mid] <= p0) lo = mid; else hi = mid - 1u;
-    }
-    uint8_t b[16];
-    uint32_t g = lo;
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-        const uint32_t p = p0 + j;
-        while (g + 1u < m && s_off[g + 1u] <= p) g++;
-        b[j] = s_chr[g];
-    }
-    if (p0 + 16u <= n && (((uintptr_t)(out + p0)) & 15u) == 0) {
-        uint4 v;
-        memcpy(&v, b, 16);
-        *(uint4 *)(out + p0) = v;
-    } else {
-        for (int j = 0; j < 16 && p0 + j < n; j++) out[p0 + j] = b[j];
+    fill_run(out, b0, b1, (uint8_t)gchar[g]);
+}
+
+// One CTA per listed long run (the count is read on the device: no host sync).
+__global__ void k_run_fill_long(uint8_t *out, const uint32_t *goff, const uint16_t *gchar, const uint32_t *longs,
+                                const uint32_t *nlong, uint32_t long_cap)
+{
+    const uint32_t cnt = min(*nlong, long_cap);
+    for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
+        const uint32_t g = longs[i];
+        const uint32_t b0 = goff[g], b1 = goff[g + 1];
+        const uint8_t c = (uint8_t)gchar[g];
+        // head bytes to the first 16-byte boundary, then striped 16-byte stores
+        uint32_t a0 = b0;
+        while (a0 < b1 && (((uintptr_t)(out + a0)) & 15u)) a0++;
+        if (threadIdx.x < a0 - b0) out[b0 + threadIdx.x] = c;
+        const uint32_t nv = (b1 - a0) / 16u;
+        const uint32_t w = (uint32_t)c * 0x01010101u;
+        const uint4 v = make_uint4(w, w, w, w);
+        for (uint32_t j = threadIdx.x; j < nv; j += blockDim.x) *(uint4 *)(out + a0 + 16u * j) = v;
+        const uint32_t t0 = a0 + 16u * nv;
+        if (threadIdx.x < b1 - t0) out[t0 + threadIdx.x] = c;
     }
 }
 
@@ -474,12 +474,15 @@ void run_assembly(Storage *st, const uint8_t *dT, uint32_t n, int W, Phrases &ph
     k_primary_index<<<grid_for(ph.z, 256), 256, 0, st->stream>>>(
         PrimaryArgs{ph.pid, pord.isa, ph.doff, ph.dlen, grp_of, goff, ph.z, st->d_flags + 2});
     after_launch(st);
-    uint32_t *tile_first = slot<uint32_t>(st, S_TILEG, grid_for(n, RF_TILE) + 1);
-    k_tile_first<<<grid_for(G, 256), 256, 0, st->stream>>>(goff, G, tile_first);
-    after_launch(st);
+    const uint32_t long_cap = n / RF_LONG + 1u;
+    uint32_t *longs = slot<uint32_t>(st, S_TILEG, long_cap);
+    check_cuda(cudaMemsetAsync(st->d_flags + 5, 0, 4, st->stream));
     probe_begin(st, GBWT_PROBE_RUN_FILL);
-    k_run_fill<<<grid_for(n, RF_TILE), RF_THREADS, 0, st->stream>>>(dOut, n, goff, G, gchar, gmix, tile_first);
-    probe_end(st, GBWT_PROBE_RUN_FILL, (uint64_t)n + 7ull * G);
+    k_run_fill_groups<<<grid_for(G, 256), 256, 0, st->stream>>>(dOut, n, goff, G, gchar, gmix, longs, long_cap,
+                                                                st->d_flags);
+    probe_end(st, GBWT_PROBE_RUN_FILL, (uint64_t)(n - M) + 7ull * G);
+    after_launch(st);
+    k_run_fill_long<<<st->num_sms * 4, 256, 0, st->stream>>>(dOut, goff, gchar, longs, st->d_flags + 5, long_cap);
     after_launch(st);
     stage_mark(st, 5);
     if (B == 0) return;

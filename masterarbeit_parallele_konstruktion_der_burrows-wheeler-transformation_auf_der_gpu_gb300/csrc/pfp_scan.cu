@@ -50,14 +50,18 @@ __host__ __device__ constexpr uint32_t pow2_mod(int W, int P)
 // Byte checks of one thread's 16 bytes (K:130-132) on whole 32-bit words.
 __device__ __forceinline__ void check_words(const uint32_t *w, uint32_t hi, bool &bad, bool &small_bad)
 {
-    const uint32_t hi4 = hi * 0x01010101u;
+    // a byte b is < 2 iff b & 0xFE is 0, is 255 iff ~b is 0; lane zero test:
+    // ~(((v & 0x7F..) + 0x7F..) | v | 0x7F..) sets the lane's top bit
     uint32_t b = 0, sb = 0;
 #pragma unroll
     for (int q = 0; q < TS_PER_THREAD / 4; q++) {
-        b |= __vcmpltu4(w[q], 0x02020202u) | __vcmpeq4(w[q], 0xFFFFFFFFu);
-        sb |= __vcmpgtu4(w[q], hi4);
+        const uint32_t lo = w[q] & 0xFEFEFEFEu, inv = ~w[q];
+        b |= ~(((lo & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | lo | 0x7F7F7F7Fu);
+        b |= ~(((inv & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | inv | 0x7F7F7F7Fu);
+        if (hi == 15u) sb |= w[q] & 0xF0F0F0F0u;
+        else if (hi < 254u) sb |= __vcmpgtu4(w[q], hi * 0x01010101u);
     }
-    bad = b != 0;
+    bad = (b & 0x80808080u) != 0;
     small_bad = sb != 0;
 }
 
@@ -122,6 +126,40 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
     if (a.n < (uint32_t)W) return 0;
     const size_t last_valid = (size_t)a.n - (size_t)W;   // last window start
     if (s0 > last_valid) return 0;
+    // windows j of this thread that may trigger: s0+j >= 1 and s0+j <= last_valid
+    uint32_t range = (last_valid - s0 >= (size_t)TS_PER_THREAD - 1) ? 0xFFFFu
+                                                                    : (1u << (uint32_t)(last_valid - s0 + 1)) - 1u;
+    if (s0 == 0) range &= ~1u;
+
+    if constexpr (WT == 5 && PT == 16) {
+        // Packed byte arithmetic, four windows per 32-bit word.  Window s
+        // hashes 8 T[s+1] + 4 T[s+2] + 2 T[s+3] + T[s+4] (mod 16): the weight
+        // of T[s] is 2^4 = 0 mod 16.  Each term reduced mod 16 before its
+        // shift keeps every byte lane below 64, so one 32-bit add serves four
+        // windows.  The first-word test is an OR of byte-wise XORs with the
+        // broadcast first five bytes.  A lane is zero exactly when
+        // ~(((v & 0x7F..) + 0x7F..) | v | 0x7F..) has its top bit set.
+        uint32_t f[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) f[k] = (uint32_t)s_fw[k] * 0x01010101u;
+        uint32_t m = 0;
+#pragma unroll
+        for (int q = 0; q < TS_PER_THREAD / 4; q++) {
+            const uint32_t x0 = w[q], x4 = w[q + 1];
+            const uint32_t x1 = __funnelshift_r(x0, x4, 8);
+            const uint32_t x2 = __funnelshift_r(x0, x4, 16);
+            const uint32_t x3 = __funnelshift_r(x0, x4, 24);
+            const uint32_t hsum = (((x1 & 0x01010101u) << 3) + ((x2 & 0x03030303u) << 2) +
+                                   ((x3 & 0x07070707u) << 1) + (x4 & 0x0F0F0F0Fu)) & 0x0F0F0F0Fu;
+            const uint32_t e = (x0 ^ f[0]) | (x1 ^ f[1]) | (x2 ^ f[2]) | (x3 ^ f[3]) | (x4 ^ f[4]);
+            const uint32_t zh = ~(((hsum & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | hsum | 0x7F7F7F7Fu);
+            const uint32_t ze = ~(((e & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | e | 0x7F7F7F7Fu);
+            // lane top bits (bits 7, 15, 23, 31) -> four mask bits
+            const uint32_t lanes = ((zh | ze) >> 7) & 0x01010101u;
+            m |= ((lanes * 0x00204081u) >> 21 & 0xFu) << (4 * q);
+        }
+        return m & range;
+    }
 
     // hash of the first window: sum b[i] * 2^(W-1-i) mod P
     uint32_t h = 0;
@@ -151,10 +189,6 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
     }
     const uint64_t regmask = (WT > 0 && WT < 8) ? ((1ull << (8 * (WT > 0 ? WT : 1))) - 1ull) : ~0ull;
 
-    // windows j of this thread that may trigger: s0+j >= 1 and s0+j <= last_valid
-    uint32_t range = (last_valid - s0 >= (size_t)TS_PER_THREAD - 1) ? 0xFFFFu
-                                                                    : (1u << (uint32_t)(last_valid - s0 + 1)) - 1u;
-    if (s0 == 0) range &= ~1u;
     const uint32_t wW = (WT > 0 && PT > 0) ? pow2_mod(WT > 0 ? WT : 1, PT > 0 ? PT : 1) : a.wW;
     uint32_t mask = 0;
 #pragma unroll
@@ -182,17 +216,55 @@ __device__ __forceinline__ uint32_t tile_triggers(const ScanArgs &a, const uint8
     return mask & range;
 }
 
-template <int WT, int PT, bool WRITE>
+// SUB consecutive 4096-window tiles per CTA: all of their bytes are loaded
+// before any is used, so more bytes are in flight per SM than with one tile
+// (the scan is otherwise latency-bound on its load).  Trigger order is tile
+// by tile, thread by thread: the write pass scans the SUB per-thread counts as
+// 16-bit lanes of one 64-bit value.
+template <int WT, int PT, bool WRITE, int SUB>
 __global__ void __launch_bounds__(TS_THREADS) k_trigger(ScanArgs a, uint32_t *counts, const uint32_t *offsets,
                                                         uint32_t *D)
 {
-    __shared__ __align__(16) uint8_t s[TS_TILE + TS_MAXW + 64];
+    static_assert(SUB >= 1 && SUB <= 4, "the write pass packs SUB counts into 16-bit lanes");
+    __shared__ __align__(16) uint8_t s[SUB * TS_TILE + TS_MAXW + 64];
     __shared__ uint8_t s_fw[TS_MAXW];
-    __shared__ uint32_t s_warp[32];
+    __shared__ uint64_t s_warp[32];
     const int W = WT > 0 ? WT : a.W;
-    const size_t base = (size_t)blockIdx.x * TS_TILE;
+    const size_t base = (size_t)blockIdx.x * (SUB * TS_TILE);
     const int halo16 = (W - 1 + 15) / 16 + 1;
-    stage_tile(a, s, base, halo16);
+    {
+        // the CTA's SUB tiles, one 16-byte vector per thread and tile, all
+        // loads issued first; then the halo past the last tile
+        const bool aligned = (((uintptr_t)a.T) & 15u) == 0;
+        uint4 v[SUB];
+#pragma unroll
+        for (int k = 0; k < SUB; k++) {
+            const size_t p = base + ((size_t)k * TS_THREADS + threadIdx.x) * 16;
+            if (aligned && p + 16 <= a.n) {
+                v[k] = __ldg((const uint4 *)(a.T + p));
+            } else {
+                uint8_t bb[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) bb[j] = (p + j < a.n) ? __ldg(a.T + p + j) : 0;
+                memcpy(&v[k], bb, 16);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < SUB; k++) *(uint4 *)(s + ((size_t)k * TS_THREADS + threadIdx.x) * 16) = v[k];
+        for (int h = threadIdx.x; h < halo16; h += TS_THREADS) {
+            const size_t p = base + (size_t)SUB * TS_TILE + (size_t)h * 16;
+            uint4 val;
+            if (aligned && p + 16 <= a.n) {
+                val = __ldg((const uint4 *)(a.T + p));
+            } else {
+                uint8_t bb[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) bb[j] = (p + j < a.n) ? __ldg(a.T + p + j) : 0;
+                memcpy(&val, bb, 16);
+            }
+            *(uint4 *)(s + (size_t)SUB * TS_TILE + (size_t)h * 16) = val;
+        }
+    }
     if (threadIdx.x < (unsigned)W) s_fw[threadIdx.x] = threadIdx.x < a.n ? __ldg(a.T + threadIdx.x) : 1;
     __syncthreads();
 
@@ -202,27 +274,47 @@ __global__ void __launch_bounds__(TS_THREADS) k_trigger(ScanArgs a, uint32_t *co
         fp0 = fp0 * FP_BASE + s_fw[i];
         fp_pow *= FP_BASE;
     }
-    uint32_t mask = tile_triggers<WT, PT>(a, s, s_fw, fw_packed, fp0, fp_pow, base, !WRITE);
-    uint32_t cnt = __popc(mask), total;
-    uint32_t ex = block_excl_scan<uint32_t, OpAdd>(cnt, total, OpAdd(), s_warp);
+    uint32_t mask[SUB];
+    uint64_t packed = 0;
+#pragma unroll
+    for (int k = 0; k < SUB; k++) {
+        mask[k] = tile_triggers<WT, PT>(a, s + (size_t)k * TS_TILE, s_fw, fw_packed, fp0, fp_pow,
+                                         base + (size_t)k * TS_TILE, !WRITE);
+        packed |= (uint64_t)__popc(mask[k]) << (16 * k);
+    }
+    uint64_t total;
+    const uint64_t ex = block_excl_scan<uint64_t, OpAdd>(packed, total, OpAdd(), s_warp);
     if (!WRITE) {
-        if (threadIdx.x == 0) counts[blockIdx.x] = total;
+        if (threadIdx.x == 0) {
+            uint32_t c = 0;
+#pragma unroll
+            for (int k = 0; k < SUB; k++) c += (uint32_t)(total >> (16 * k)) & 0xFFFFu;
+            counts[blockIdx.x] = c;
+        }
         return;
     }
-    uint32_t o = offsets[blockIdx.x] + ex;
-    const uint32_t s0 = (uint32_t)(base + (size_t)threadIdx.x * TS_PER_THREAD);
-    while (mask) {
-        int j = __ffs(mask) - 1;
-        mask &= mask - 1;
-        D[o++] = s0 + (uint32_t)j + (uint32_t)W - 1u;
+    uint32_t tile_base = offsets[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SUB; k++) {
+        uint32_t o = tile_base + ((uint32_t)(ex >> (16 * k)) & 0xFFFFu);
+        const uint32_t s0 = (uint32_t)(base + (size_t)k * TS_TILE + (size_t)threadIdx.x * TS_PER_THREAD);
+        uint32_t m = mask[k];
+        while (m) {
+            const int j = __ffs(m) - 1;
+            m &= m - 1;
+            D[o++] = s0 + (uint32_t)j + (uint32_t)W - 1u;
+        }
+        tile_base += (uint32_t)(total >> (16 * k)) & 0xFFFFu;
     }
 }
+
+constexpr int TS_SUB = 4;      // tiles per CTA in the pipeline's scan
 
 template <int WT, int PT>
 static void launch_pair(Storage *st, const ScanArgs &a, unsigned blocks, uint32_t *counts, uint32_t *&D)
 {
     probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
-    k_trigger<WT, PT, false><<<blocks, TS_THREADS, 0, st->stream>>>(a, counts, nullptr, nullptr);
+    k_trigger<WT, PT, false, TS_SUB><<<blocks, TS_THREADS, 0, st->stream>>>(a, counts, nullptr, nullptr);
     probe_end(st, GBWT_PROBE_TRIGGER_SCAN, a.n);
     after_launch(st);
     // exclusive scan of block counts; total -> d_scalars[0]
@@ -238,7 +330,7 @@ static void launch_pair(Storage *st, const ScanArgs &a, unsigned blocks, uint32_
     uint32_t c = (uint32_t)(st->h_scalars[0] & 0xFFFFFFFFu);
     D = slot<uint32_t>(st, S_D, (size_t)c + 1);
     probe_begin(st, GBWT_PROBE_TRIGGER_SCAN);
-    k_trigger<WT, PT, true><<<blocks, TS_THREADS, 0, st->stream>>>(a, nullptr, counts, D);
+    k_trigger<WT, PT, true, TS_SUB><<<blocks, TS_THREADS, 0, st->stream>>>(a, nullptr, counts, D);
     probe_end(st, GBWT_PROBE_TRIGGER_SCAN, (uint64_t)a.n + 4ull * c);
     after_launch(st);
     k_set_u32<<<1, 1, 0, st->stream>>>(D + c, a.n + (uint32_t)a.W - 1u);
@@ -255,7 +347,7 @@ uint32_t run_trigger_scan(Storage *st, const uint8_t *dT, uint32_t n, int W, int
     a.wW = wW;
     a.hi = small ? 15u : 254u;
     a.flags = st->d_flags;
-    unsigned blocks = grid_for(n, TS_TILE);
+    unsigned blocks = grid_for(n, TS_TILE * TS_SUB);
     uint32_t *counts = slot<uint32_t>(st, S_TMP0, blocks + 1);
     if (W == 5 && P == 16) launch_pair<5, 16>(st, a, blocks, counts, D);
     else if (W == 5 && P == 11) launch_pair<5, 11>(st, a, blocks, counts, D);
@@ -602,7 +694,7 @@ static int64_t noalloc_launch(const ScanArgs &a, unsigned blocks, uint32_t *scra
     check_cuda(cudaMemsetAsync(words, 0, 64 * sizeof(uint32_t), stream));
     ScanArgs b = a;
     b.flags = words;
-    k_trigger<WT, PT, false><<<blocks, TS_THREADS, 0, stream>>>(b, counts, nullptr, nullptr);
+    k_trigger<WT, PT, false, 1><<<blocks, TS_THREADS, 0, stream>>>(b, counts, nullptr, nullptr);
     check_cuda(cudaGetLastError());
     const unsigned tiles = (blocks + SC_TILE - 1) / SC_TILE;
     if (tiles == 1) {
@@ -625,7 +717,7 @@ static int64_t noalloc_launch(const ScanArgs &a, unsigned blocks, uint32_t *scra
     if (host_words[0] & ERR_SMALL_RANGE) return GBWT_UNSUPPORTED_INPUT;
     const uint32_t c = host_words[1];
     if ((int64_t)c + 1 > capacity) return GBWT_BAD_PARAMETER;
-    k_trigger<WT, PT, true><<<blocks, TS_THREADS, 0, stream>>>(b, nullptr, counts, D);
+    k_trigger<WT, PT, true, 1><<<blocks, TS_THREADS, 0, stream>>>(b, nullptr, counts, D);
     k_set_u32<<<1, 1, 0, stream>>>(D + c, a.n + (uint32_t)a.W - 1u);
     check_cuda(cudaGetLastError());
     check_cuda(cudaStreamSynchronize(stream));
