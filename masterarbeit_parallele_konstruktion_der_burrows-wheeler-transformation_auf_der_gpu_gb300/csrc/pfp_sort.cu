@@ -1094,24 +1094,32 @@ struct StoreBucket {
     uint64_t *bst;
     __device__ __forceinline__ void operator()(size_t r, uint64_t pre, uint64_t) const { bst[r] = pre; }
 };
-__global__ void k_bucket_scatter(const uint32_t *pid, const uint32_t *lexrank, const uint64_t *bst,
-                                 const uint32_t *occ, uint32_t z, uint32_t *cur, uint32_t *isa, uint32_t *sa,
-                                 uint32_t *act_x, uint32_t *act_g, uint32_t *flags)
+// Per phrase: (bucket start, active-list start), the second 0xFFFFFFFF for a
+// phrase that occurs once.  One random lookup per occurrence instead of three
+// (rank, bucket, count) in the scatter below.
+__global__ void k_bucket_info(const uint32_t *lexrank, const uint64_t *bst, const uint32_t *occ, uint32_t d,
+                              uint2 *info)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= d) return;
+    const uint64_t p = bst[lexrank[q]];
+    info[q] = make_uint2((uint32_t)(p >> 32), occ[q] > 1u ? (uint32_t)p : 0xFFFFFFFFu);
+}
+__global__ void k_bucket_scatter(const uint32_t *pid, const uint2 *info, uint32_t z, uint32_t *cur, uint32_t *isa,
+                                 uint32_t *sa, uint32_t *act_x, uint32_t *act_g, uint32_t *flags)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= z) return;
     const uint32_t q = pid[i];
-    const uint32_t r = lexrank[q];
-    const uint64_t p = bst[r];
-    const uint32_t b = (uint32_t)(p >> 32);
+    const uint2 inf = info[q];
+    const uint32_t b = inf.x;
     isa[i] = b;
-    if (occ[q] == 1u) {
+    if (inf.y == 0xFFFFFFFFu) {
         if (b < z) sa[b] = i;         // the only suffix starting with this phrase
         else atomicOr(flags, ERR_INTERNAL);
     } else {
-        const uint32_t k = atomicAdd(cur + r, 1u);
-        const uint32_t pos = (uint32_t)p + k;
-        if (k < occ[q] && pos < z) {
+        const uint32_t pos = inf.y + atomicAdd(cur + q, 1u);
+        if (pos < z) {
             act_x[pos] = i;
             act_g[pos] = b;
         } else {
@@ -1151,8 +1159,11 @@ void run_parse_sa(Storage *st, Phrases &ph, DictOrder &dord, ParseOrder &pord)
     check_cuda(cudaMemsetAsync(st->d_scalars, 0, 8, st->stream));
     device_scan<uint64_t, OpAdd>(st, d, LoadBucket{cnt_r}, StoreBucket{bst}, false, (uint64_t *)st->d_scalars);
     check_cuda(cudaMemsetAsync(cur, 0, (size_t)d * 4, st->stream));
-    k_bucket_scatter<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, dord.lexrank, bst, ph.occ, z, cur, pord.isa,
-                                                               pord.sa, act_x, act_g, st->d_flags);
+    uint2 *info = slot<uint2>(st, S_KEY0, d);
+    k_bucket_info<<<grid_for(d, 256), 256, 0, st->stream>>>(dord.lexrank, bst, ph.occ, d, info);
+    after_launch(st);
+    k_bucket_scatter<<<grid_for(z, 256), 256, 0, st->stream>>>(ph.pid, info, z, cur, pord.isa, pord.sa, act_x, act_g,
+                                                               st->d_flags);
     after_launch(st);
     fetch_scalars(st, 1);
     const uint64_t tot = st->h_scalars[0];
