@@ -120,7 +120,11 @@ __global__ void __launch_bounds__(PH_THREADS) k_phrase_hash(HashArgs a)
     uint32_t pos = (uint32_t)((key * 0xD6E8FEB86659FD93ull) >> (64 - a.logc));
     bool ok = false;
     for (uint32_t probe = 0; probe <= a.cmask; probe++) {
-        unsigned long long cur = atomicCAS(a.tkeys + pos, 0ull, (unsigned long long)key);
+        // a plain read first: in a repetitive text most occurrences find
+        // their key already in place, and a load costs L2 less than a CAS
+        // (keys are never removed, so a key seen once stays)
+        unsigned long long cur = __ldcg(a.tkeys + pos);
+        if (cur == 0ull) cur = atomicCAS(a.tkeys + pos, 0ull, (unsigned long long)key);
         if (cur == 0ull) {
             // the inserting occurrence is the slot's representative
             a.tvals[pos] = k;

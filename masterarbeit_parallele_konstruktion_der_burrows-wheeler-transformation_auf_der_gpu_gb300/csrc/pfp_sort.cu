@@ -476,11 +476,16 @@ __device__ __forceinline__ void warp_group(uint64_t *key, uint32_t s, uint32_t g
 // both lists in no particular order), and tbig[b] = the start of the one that
 // starts in tile b (a tile holds at most one: such a group is longer than a
 // tile).
-__global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
-                               uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart, uint32_t *bigs,
-                               uint32_t big_cap, uint32_t *tbig)
+__global__ void k_round_gather(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A_arg,
+                               const uint32_t *Ap, uint32_t h, uint32_t *key2, uint32_t *flags, uint32_t *tstart,
+                               uint32_t *bigs, uint32_t big_cap, uint32_t *tbig, uint32_t *hist)
 {
+    // the active count: a launch argument when the host knows it, else read
+    // on the device (the grid then covers an upper bound)
+    const uint32_t A = Ap ? *Ap : A_arg;
+    if (hist && blockIdx.x == 0 && threadIdx.x == 0) *hist = A;
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x >= A) return;
     bool gnew = false;
     if (a < A) {
         key2[a] = isa[act_x[a] + h] + 1u;
@@ -517,8 +522,8 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
                                                             const uint32_t *__restrict__ act_g,
                                                             const uint32_t *__restrict__ key2,
                                                             const uint32_t *__restrict__ tstart,
-                                                            const uint32_t *__restrict__ tbig, uint32_t A,
-                                                            uint32_t h2, Rem rem, uint32_t *isa, uint32_t *sa,
+                                                            const uint32_t *__restrict__ tbig, uint32_t A_arg,
+                                                            const uint32_t *__restrict__ Ap, uint32_t h2, Rem rem, uint32_t *isa, uint32_t *sa,
                                                             uint32_t *out_x, uint32_t *out_g, uint32_t *counter,
                                                             uint32_t *flags, bool collect_stats)
 {
@@ -537,6 +542,9 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
 
     // the CTA's elements: from the first group start in its tile to the
     // first group start in the next tile (or A)
+    const uint32_t A = Ap ? *Ap : A_arg;             // from the device: the grid covers an upper bound
+    const uint32_t tiles = (A + SS_TILE - 1) / SS_TILE;
+    if (blockIdx.x >= tiles) return;
     const uint32_t s0 = tstart[blockIdx.x];
     if (s0 == 0xFFFFFFFFu) return;                   // no group starts in this tile
     uint32_t e1;
@@ -547,10 +555,10 @@ __global__ void __launch_bounds__(SS_THREADS, 2) k_seg_sort(const uint32_t *__re
         // sorts it
         e1 = bstart;
     } else {
-        e1 = blockIdx.x + 1 < gridDim.x ? tstart[blockIdx.x + 1] : A;
+        e1 = blockIdx.x + 1 < tiles ? tstart[blockIdx.x + 1] : A;
         if (e1 == 0xFFFFFFFFu) {
             // only the last tile, partly filled, may lack a start
-            if (blockIdx.x + 2 < gridDim.x) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
+            if (blockIdx.x + 2 < tiles) { if (threadIdx.x == 0) atomicOr(flags, ERR_INTERNAL); return; }
             e1 = A;
         }
     }
@@ -787,7 +795,7 @@ struct StoreBigActive {
 template <typename Rem>
 static void big_groups(Storage *st, uint32_t N, uint32_t nbig, const uint32_t *dbigs, uint32_t big_cap, uint32_t h2,
                        const uint32_t *key2, const uint32_t *act_x, const uint32_t *act_g, Rem rem, uint32_t *isa,
-                       uint32_t *sa, uint32_t *out_x, uint32_t *out_g)
+                       uint32_t *sa, uint32_t *out_x, uint32_t *out_g, const uint32_t *counter, uint32_t *big_total)
 {
     // starts and ends, both sorted: big groups are disjoint ranges, so the
     // i-th start and the i-th end delimit the i-th group
@@ -822,43 +830,76 @@ static void big_groups(Storage *st, uint32_t N, uint32_t nbig, const uint32_t *d
     ActiveTest<Rem> t{k, v, total, h2, rem};
     device_scan<uint64_t, OpMax2>(st, total, LoadRoundHead{k, lb}, StoreBigRound<Rem>{t, lb, bhead, isa, head, sa},
                                   true, (uint64_t *)nullptr);
-    check_cuda(cudaMemsetAsync(st->d_scalars + 1, 0, 8, st->stream));
+    check_cuda(cudaMemsetAsync(big_total, 0, 4, st->stream));
     device_scan<uint32_t, OpAdd>(st, total, LoadActive<Rem>{t},
-                                 StoreBigActive<Rem>{t, head, (const uint32_t *)st->d_scalars, out_x, out_g}, false,
-                                 (uint32_t *)(st->d_scalars + 1));
+                                 StoreBigActive<Rem>{t, head, counter, out_x, out_g}, false, big_total);
 }
+
+__global__ void k_add_u32(uint32_t *dst, const uint32_t *src) { *dst += *src; }
+__global__ void k_set_word(uint32_t *dst, uint32_t v) { *dst = v; }
 
 // Prefix-doubling rounds from prefix length h with A active elements listed
 // group by group in act_x (suffix) / act_g (group head); isa holds every
 // suffix's group head and sa every finished slot.  Returns the rounds run.
+//
+// The active count of each round stays on the device (two counters used in
+// turn: the kernels of round r read round r-1's and the segmented kernel
+// counts into the other one); launches are sized by the last count the host
+// read, an upper bound since the count only shrinks.  The host reads the
+// count back only every DR_SYNC rounds once fewer than DR_SYNC_MIN elements
+// are active (and in rounds with groups above the shared-memory limit, whose
+// side path is sized on the host), so small sorts run their rounds back to
+// back; rounds launched after the count reached zero exit at once.  Large
+// rounds read it every time: launches sized by a stale count cost more there
+// (measured on the 512 MiB text: +0.3 ms with reads every 4th round only).
+constexpr int DR_SYNC = 4;
+constexpr uint32_t DR_SYNC_MIN = 1u << 20;
+constexpr int DR_MAXR = 40;      // rounds recorded (h doubles each round: at most 33)
 template <typename Rem>
 static int doubling_rounds(Storage *st, uint32_t N, uint64_t h, uint32_t A, Rem rem, uint32_t *isa, uint32_t *sa,
                            uint32_t *act_x, uint32_t *act_g, uint32_t *act_x2, uint32_t *act_g2, bool check_big)
 {
-    int rounds = 0;
     static bool ss_attr = false;
     if (!ss_attr) {
         check_cuda(cudaFuncSetAttribute(k_seg_sort<Rem>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SS_SMEM));
         ss_attr = true;
     }
     const bool debug = getenv("GBWT_DEBUG") != nullptr;
-    // groups only split: once a round has no group above SS_SEGMAX, no later
-    // round has one, and the big-group listing (and its host round trip) stops
-    while (A > 0) {
-        if (h >= N) throw Error{GBWT_INTERNAL_ERROR};
+    // device words: [0], [1] the two round counters, [2] the side path's
+    // count, [8 + r] the active count round r started with
+    uint32_t *dw = (uint32_t *)(st->d_scalars + 16);
+    const uint32_t *hw = (const uint32_t *)(st->h_scalars + 160);   // pinned words past the byte tables
+    check_cuda(cudaMemsetAsync(dw, 0, (8 + DR_MAXR) * 4, st->stream));
+    k_set_word<<<1, 1, 0, st->stream>>>(dw + 1, A);     // round 0's count, read by round 1's kernels
+    after_launch(st);
+    uint32_t A_ub = A;
+    bool exact = true;               // A_ub is the count itself, not a bound
+    int r = 0;
+    while (A_ub > 0) {
+        if (r >= DR_MAXR) throw Error{GBWT_INTERNAL_ERROR};
+        uint32_t *Aprev = dw + ((r + 1) & 1), *Acur = dw + (r & 1);
+        if (h >= N) {
+            // only legal when every suffix is finished already
+            check_cuda(cudaMemcpyAsync(st->h_scalars + 160, dw, 8, cudaMemcpyDeviceToHost, st->stream));
+            check_cuda(cudaStreamSynchronize(st->stream));
+            if (hw[(r + 1) & 1] != 0) throw Error{GBWT_INTERNAL_ERROR};
+            break;
+        }
         const uint32_t h2 = (uint32_t)(2 * h < 0xFFFFFFFFull ? 2 * h : 0xFFFFFFFFull);
         // gather this round's keys before any rank changes; list big groups
         uint32_t *key2 = slot<uint32_t>(st, S_TMP2, N);
-        const uint32_t ss_tiles = grid_for(A, SS_TILE);
+        const uint32_t ss_tiles = grid_for(A_ub, SS_TILE);
         uint32_t *tstart = slot<uint32_t>(st, S_SSTART, (size_t)ss_tiles * 2);
         uint32_t *tbig = tstart + ss_tiles;
-        const uint32_t big_cap = A / SS_SEGMAX + 1u;
+        const uint32_t big_cap = A_ub / SS_SEGMAX + 1u;
         uint32_t *bigs = check_big ? slot<uint32_t>(st, S_BIGL, (size_t)big_cap * 2) : nullptr;
         if (check_big) check_cuda(cudaMemsetAsync(st->d_flags + 3, 0, 8, st->stream));
         check_cuda(cudaMemsetAsync(tstart, 0xFF, (size_t)ss_tiles * 4 * (check_big ? 2 : 1), st->stream));
         static_assert(SS_TILE % 256 == 0, "gather blocks must not straddle tiles");
-        k_round_gather<<<grid_for(A, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A, (uint32_t)h, key2,
-                                                                 st->d_flags, tstart, bigs, big_cap, tbig);
+        const uint32_t *Adev = exact ? nullptr : Aprev;     // a known count goes in as an argument
+        k_round_gather<<<grid_for(A_ub, 256), 256, 0, st->stream>>>(act_x, act_g, isa, A_ub, Adev, (uint32_t)h,
+                                                                    key2, st->d_flags, tstart, bigs, big_cap, tbig,
+                                                                    dw + 8 + r);
         after_launch(st);
         uint32_t nbig = 0;
         if (check_big) {
@@ -869,34 +910,56 @@ static int doubling_rounds(Storage *st, uint32_t N, uint64_t h, uint32_t A, Rem 
             if (nbig > big_cap || cnt[1] != nbig) throw Error{GBWT_INTERNAL_ERROR};
         }
         check_big = nbig > 0;
-        if (debug) fprintf(stderr, "gbwt: round h=%llu active=%u big groups=%u\n", (unsigned long long)h, A, nbig);
-        uint32_t *counter = (uint32_t *)st->d_scalars;
-        check_cuda(cudaMemsetAsync(st->d_scalars, 0, 16, st->stream));
+        if (debug) fprintf(stderr, "gbwt: round h=%llu active<=%u big groups=%u\n", (unsigned long long)h, A_ub, nbig);
+        check_cuda(cudaMemsetAsync(Acur, 0, 4, st->stream));
         if (debug) check_cuda(cudaMemsetAsync(st->d_flags + 16, 0, 8 * sizeof(uint32_t), st->stream));
         probe_begin(st, GBWT_PROBE_SEG_SORT);
         k_seg_sort<Rem><<<ss_tiles, SS_THREADS, SS_SMEM, st->stream>>>(
-            act_x, act_g, key2, tstart, nbig ? tbig : nullptr, A, h2, rem, isa, sa, act_x2, act_g2, counter,
+            act_x, act_g, key2, tstart, nbig ? tbig : nullptr, A_ub, Adev, h2, rem, isa, sa, act_x2, act_g2, Acur,
             st->d_flags, debug);
-        // per active element: read x, group, key (12 B); write its rank and
-        // either its next-round (x, group) or its final suffix-array slot (12 B)
-        probe_end(st, GBWT_PROBE_SEG_SORT, 24ull * A);
+        // algorithmic bytes (24 per active element) are added once the
+        // round's count is known, below
+        probe_end(st, GBWT_PROBE_SEG_SORT, 0);
         after_launch(st);
-        if (nbig) big_groups<Rem>(st, N, nbig, bigs, big_cap, h2, key2, act_x, act_g, rem, isa, sa, act_x2, act_g2);
-        fetch_scalars(st, 2);
-        if (debug) {
-            uint32_t tiers[8];
-            check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
-            fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
-                    SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
-            fprintf(stderr, "gbwt:   larger groups: one value %u, majority + <=32 outliers %u, other %u\n",
-                    tiers[4], tiers[7], tiers[6]);
+        if (nbig) {
+            big_groups<Rem>(st, N, nbig, bigs, big_cap, h2, key2, act_x, act_g, rem, isa, sa, act_x2, act_g2, Acur,
+                            dw + 2);
+            k_add_u32<<<1, 1, 0, st->stream>>>(Acur, dw + 2);
+            after_launch(st);
         }
-        A = (uint32_t)st->h_scalars[0] + (uint32_t)st->h_scalars[1];
         uint32_t *t1 = act_x; act_x = act_x2; act_x2 = t1;
         uint32_t *t2 = act_g; act_g = act_g2; act_g2 = t2;
         h *= 2;
-        rounds++;
+        r++;
+        if (check_big || nbig || debug || A_ub >= DR_SYNC_MIN || r % DR_SYNC == 0) {
+            check_cuda(cudaMemcpyAsync(st->h_scalars + 160, dw, 8, cudaMemcpyDeviceToHost, st->stream));
+            check_cuda(cudaStreamSynchronize(st->stream));
+            A_ub = hw[(r + 1) & 1];        // the count this round produced (r already advanced)
+            exact = true;
+            if (debug) {
+                uint32_t tiers[8];
+                check_cuda(cudaMemcpy(tiers, st->d_flags + 16, sizeof(tiers), cudaMemcpyDeviceToHost));
+                fprintf(stderr, "gbwt:   groups=%u elements in groups <=%u: %u, <=%u: %u, larger: %u\n", tiers[3],
+                        SS_COUNTMAX, tiers[0], SS_WARPMAX, tiers[1], tiers[2]);
+                fprintf(stderr, "gbwt:   larger groups: one value %u, majority + <=32 outliers %u, other %u\n",
+                        tiers[4], tiers[7], tiers[6]);
+            }
+        } else {
+            exact = false;
+        }
     }
+    // rounds that had work, and the probe's algorithmic bytes per round
+    check_cuda(cudaMemcpyAsync(st->h_scalars + 160, dw, (8 + DR_MAXR) * 4, cudaMemcpyDeviceToHost, st->stream));
+    check_cuda(cudaStreamSynchronize(st->stream));
+    int rounds = 0;
+    for (int i = 0; i < r; i++) {
+        const uint32_t a = hw[8 + i];
+        if (a == 0) break;
+        rounds++;
+        if (st->probe_kernel == GBWT_PROBE_SEG_SORT) st->probe_bytes += (int64_t)24 * a;
+    }
+    // launches of rounds that found nothing to do are not counted
+    if (st->probe_kernel == GBWT_PROBE_SEG_SORT) st->probe_launches -= r - rounds;
     return rounds;
 }
 
