@@ -131,8 +131,12 @@ def load_tuning(path: str | None = None) -> dict | None:
         return json.load(f)
 
 
-def tuning_for(n: int, table: dict | None) -> dict | None:
-    """The knobs of the largest size class not above n bytes (the smallest class for smaller n)."""
+_MERGED: dict = {}
+
+
+def tuning_for(n: int, table: dict | None, W: int | None = None) -> dict | None:
+    """The knobs of the largest size class not above n bytes (the smallest class for smaller n),
+    with the table's per-window-length overrides for W laid over them ({"windows": {"35": {...}}})."""
     if not table or not table.get("classes"):
         return None
     classes = sorted((int(k), v) for k, v in table["classes"].items())
@@ -140,7 +144,13 @@ def tuning_for(n: int, table: dict | None) -> dict | None:
     for mib, knobs in classes:
         if (mib << 20) <= n:
             best = knobs
-    return best
+    over = (table.get("windows") or {}).get(str(W)) if W is not None else None
+    if not over:
+        return best
+    key = (id(best), id(over))
+    if key not in _MERGED:
+        _MERGED[key] = {**best, **over}
+    return _MERGED[key]
 
 
 class JobInfo(ctypes.Structure):
@@ -264,10 +274,10 @@ class Storage:
         self._table = None
         self._set_raw(knobs)
 
-    def _auto(self, n: int) -> None:
+    def _auto(self, n: int, W: int | None = None) -> None:
         if self._table is None:
             return
-        knobs = tuning_for(int(n), self._table)
+        knobs = tuning_for(int(n), self._table, W)
         if knobs is not self._applied:
             self._set_raw(knobs)
             self._applied = knobs
@@ -309,7 +319,7 @@ class Storage:
         t = _host_u8(text)
         out = np.empty(max(len(t), 1), dtype=np.uint8)
         flags = (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (FLAG_STAGE_TIMES if stage_times else 0)
-        self._auto(len(t))
+        self._auto(len(t), W)
         _check(_lib().gbwt_pfp_bwt(self.handle, t.ctypes.data, out.ctypes.data, len(t), W, P, flags),
                "gbwt_pfp_bwt")
         return out[:len(t)]
@@ -321,7 +331,7 @@ class Storage:
                 or not out.flags.c_contiguous or len(out) < len(text):
             raise ValueError("text/out must be contiguous uint8 arrays, len(out) >= len(text)")
         flags = FLAG_SMALL_ALPHABET if small_alphabet else 0
-        self._auto(len(text))
+        self._auto(len(text), W)
         return _check(_lib().gbwt_pfp_bwt(self.handle, text.ctypes.data, out.ctypes.data, len(text), W, P, flags),
                       "gbwt_pfp_bwt")
 
@@ -410,7 +420,7 @@ class Storage:
         """Device-pointer variant: ``text_ptr``/``out_ptr`` are CUDA device addresses."""
         flags = FLAG_DEVICE_POINTERS | (FLAG_SMALL_ALPHABET if small_alphabet else 0) | (
             FLAG_STAGE_TIMES if stage_times else 0)
-        self._auto(n)
+        self._auto(n, W)
         return _check(_lib().gbwt_pfp_bwt(self.handle, ctypes.c_void_p(text_ptr), ctypes.c_void_p(out_ptr), n, W, P,
                                           flags), "gbwt_pfp_bwt")
 

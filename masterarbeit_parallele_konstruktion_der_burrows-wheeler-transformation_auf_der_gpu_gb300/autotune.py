@@ -157,6 +157,11 @@ def main(argv=None) -> int:
         log(f"class {mib} MiB")
         out["classes"][str(mib)] = tune_class(pkg, wl, mib, args.repeats, log)
     path = args.out or pkg.TUNING_FILE
+    # per-window-length overrides of an existing table are kept
+    old = pkg.load_tuning(pkg.TUNING_FILE) or {}
+    for key in ("windows", "windows_note"):
+        if key in old:
+            out[key] = old[key]
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
     print(json.dumps(out))
