@@ -1,6 +1,7 @@
 """Drop-in surfaces on the GPU: the CLI run like the reference's programs
-(input.txt -> out.txt, variant from the program name), the raw-byte fast
-path, and the libcubwt-compatible entry point."""
+(input.txt -> out.txt, program from its name: the PFP variants,
+Lyndon_Grammar_BWT and libcubwt), the raw-byte fast path, and the
+libcubwt-compatible entry point."""
 import os
 import subprocess
 
@@ -15,7 +16,7 @@ def _cli(pkg):
 
 
 @pytest.mark.parametrize("variant", ["Prefix_Free_Parsing_W=5_P=16", "Prefix_Free_Parsing_W=35_P=81_small_alphabet",
-                                     "Prefix_Free_Parsing_W=5_P=23"])
+                                     "Prefix_Free_Parsing_W=5_P=23", "Lyndon_Grammar_BWT"])
 def test_cli_as_reference_program(pkg, orc, wl, tmp_path, variant):
     t = wl.dna_copies(base_len=8 * 1024, copies=6, seed=9)
     (tmp_path / "input.txt").write_text(f"{len(t)}\n" + " ".join(map(str, t.tolist())) + "\n")
@@ -27,6 +28,44 @@ def test_cli_as_reference_program(pkg, orc, wl, tmp_path, variant):
     assert int(lines[0]) == len(t)
     got = np.array(list(map(int, lines[1].split())), dtype=np.uint8)
     assert np.array_equal(got, orc.sa_bwt(t))
+
+
+def _write_input(path, t):
+    path.write_text(f"{len(t)}\n" + " ".join(map(str, t.tolist())) + "\n")
+
+
+def _libcubwt_harness_output(L, idx):
+    # LC:2989-3020: raw layout for index 0, else L[0] moved to the index
+    # (and dropped when the index is n)
+    if idx == 0:
+        return L
+    return np.array([v for i in range(1, len(L)) for v in ((L[0], L[i]) if i == idx else (L[i],))], dtype=np.uint8)
+
+
+@pytest.mark.parametrize("case", ["any_bytes", "dna", "index_n"])
+def test_cli_as_libcubwt_program(pkg, orc, wl, tmp_path, case):
+    rng = np.random.default_rng(7)
+    if case == "any_bytes":
+        t = rng.integers(0, 256, size=5000).astype(np.uint8)
+        t[:3] = (0, 1, 255)
+    elif case == "dna":
+        t = wl.dna_copies(base_len=8 * 1024, copies=6, seed=11)
+    else:
+        t = np.array([9, 3, 3, 4, 3, 3], dtype=np.uint8)    # the whole text sorts last: index n
+    _write_input(tmp_path / "input.txt", t)
+    exe = tmp_path / "libcubwt_Linux"
+    os.symlink(_cli(pkg), exe)
+    r = subprocess.run([str(exe)], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    head, body = (tmp_path / "out.txt").read_text().split("\n", 1)
+    assert int(head) == len(t)
+    got = np.array(list(map(int, body.split())), dtype=np.uint8)
+    L, idx = _libcubwt_expected(orc, t)
+    if case == "index_n":
+        assert idx == len(t)
+    assert np.array_equal(got, _libcubwt_harness_output(L, idx))
+    if case == "dna":
+        assert np.array_equal(got, orc.sa_bwt(t))     # valid PFP input: the same bytes as the PFP programs
 
 
 def test_cli_binary_fast_path(pkg, orc, wl, tmp_path):
