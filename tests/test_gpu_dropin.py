@@ -46,7 +46,9 @@ def _libcubwt_harness_output(L, idx):
 def test_cli_as_libcubwt_program(pkg, orc, wl, tmp_path, case):
     rng = np.random.default_rng(7)
     if case == "any_bytes":
-        t = rng.integers(0, 256, size=5000).astype(np.uint8)
+        # 0, 1 and 255 included; at most 253 distinct values (gbwt_libcubwt_bwt's contract)
+        vals = np.array([v for v in range(256) if v not in (100, 101, 102)], dtype=np.uint8)
+        t = vals[rng.integers(0, len(vals), size=5000)]
         t[:3] = (0, 1, 255)
     elif case == "dna":
         t = wl.dna_copies(base_len=8 * 1024, copies=6, seed=11)
