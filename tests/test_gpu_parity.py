@@ -167,3 +167,29 @@ def test_device_pointer_path(pkg, orc, wl):
         st.pfp_bwt_device(dt.data_ptr(), dout.data_ptr(), len(t), 5, 16)
         torch.cuda.synchronize()
         assert np.array_equal(dout.cpu().numpy(), orc.sa_bwt(t))
+
+
+def test_pinned_host_buffers(storage, orc, wl):
+    # pinned host buffers (asynchronous copies) give the same bytes as
+    # pageable ones, also for texts without mixed blocks
+    torch = pytest.importorskip("torch")
+    cases = list(_cases(seed=77, count=40, max_n=3000))
+    cases.append(wl.dna_copies(base_len=64 * 1024, copies=16, seed=21))
+    cases.append(np.full(5000, 7, dtype=np.uint8))
+    for t in cases:
+        ht = torch.from_numpy(t.copy()).pin_memory()
+        ho = torch.full((len(t),), 1, dtype=torch.uint8).pin_memory()
+        storage.pfp_bwt_into(ht.numpy(), ho.numpy(), 5, 16)
+        want, _ = orc.pfp_bwt(t, 5, 16)
+        assert np.array_equal(ho.numpy(), want), (len(t), t[:20].tolist())
+        assert np.array_equal(storage.pfp_bwt(t, 5, 16), want)
+
+
+def test_stage_times_add_up(storage, wl):
+    # every stage gets its own time and the parts add up to the total
+    t = wl.dna_copies(base_len=128 * 1024, copies=32, seed=22)
+    storage.pfp_bwt(t, 5, 16, stage_times=True)
+    ms = storage.stats()["stage_ms"]
+    parts = [ms[k] for k in ("scan", "phrases", "dictionary", "parse_sa", "s_groups", "runs", "mixed")]
+    assert all(v > 0 for v in parts), ms
+    assert abs(sum(parts) - ms["total"]) <= 0.02 * ms["total"] + 0.01, ms
