@@ -81,6 +81,18 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_timing(ms, e2e_ms, ws, n, device):
+    """One text per rank (replicas, no exchange between ranks): the step time of
+    the job is the slowest rank's (max over ranks), the throughput every rank's
+    text over it.  Returns (ms, e2e_ms, MB/s, e2e MB/s)."""
+    if ws > 1:
+        import torch
+        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    return ms, e2e_ms, ws * n / (ms / 1000.0) / 1e6, ws * n / (e2e_ms / 1000.0) / 1e6
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -539,16 +551,11 @@ def run_gpu(args):
     if not np.array_equal(dev_out.cpu().numpy(), got):
         raise SystemExit("bench: device and host paths differ")
 
-    if ws > 1:
-        t = torch.tensor([ms, e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
+    ms, e2e_ms, value, e2e_value = replica_timing(ms, e2e_ms, ws, n, "cuda")
     if rank != 0:
         torch.distributed.destroy_process_group()
         return 0
 
-    value = ws * n / (ms / 1000.0) / 1e6
-    e2e_value = ws * n / (e2e_ms / 1000.0) / 1e6
     peak, peak_kind = measured_peak()
     roofline = roofline_of(probe, "k_seg_sort", "k_seg_sort<ParseRem/DictRem> (prefix-doubling rounds in CTAs)",
                            peak, peak_kind, args.steps, ms)
