@@ -541,6 +541,13 @@ def pfp_bwt(text, W: int = 5, P: int = 16, small_alphabet: bool = False) -> np.n
     return default_storage().pfp_bwt(text, W, P, small_alphabet)
 
 
+# The reference's Lyndon-grammar program writes the same BWT (its output is
+# compared with libcubwt's, compare_script_lyndon.sh); here the PFP pipeline
+# builds it with these parameters.
+LYNDON_PROGRAM = "Lyndon_Grammar_BWT"
+LYNDON_VARIANT = (5, 16, False)
+
+
 def variant(name: str) -> tuple[int, int, bool]:
     """(W, P, small_alphabet) of a reference binary name (with or without _Linux)."""
     base = os.path.basename(name)
@@ -548,6 +555,8 @@ def variant(name: str) -> tuple[int, int, bool]:
         base = base[: -len("_Linux")]
     if base.endswith(".cu"):
         base = base[:-3]
+    if base == LYNDON_PROGRAM:
+        return LYNDON_VARIANT
     return VARIANTS[base]
 
 

@@ -70,6 +70,7 @@ def test_no_gpu_fails_loudly(pkg):
 def test_variant_names(pkg):
     assert pkg.variant("Prefix_Free_Parsing_W=35_P=81_small_alphabet_Linux") == (35, 81, True)
     assert pkg.variant("./Prefix_Free_Parsing_W=5_P=13_Linux") == (5, 13, False)
+    assert pkg.variant("Lyndon_Grammar_BWT_Linux") == (5, 16, False)     # same BWT, built by PFP
     assert len(pkg.VARIANTS) == 9
 
 
