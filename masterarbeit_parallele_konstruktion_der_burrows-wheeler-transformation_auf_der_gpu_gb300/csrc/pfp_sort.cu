@@ -161,17 +161,6 @@ struct StoreHeadActive0 {
     }
 };
 
-// Round keys: (group head, isa[x+h] + 1).
-__global__ void k_round_keys(const uint32_t *act_x, const uint32_t *act_g, const uint32_t *isa, uint32_t A,
-                             uint32_t h, int lb, uint64_t *keys, uint32_t *vals)
-{
-    uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= A) return;
-    const uint32_t x = act_x[a];
-    keys[a] = ((uint64_t)act_g[a] << lb) | (uint64_t)(isa[x + h] + 1u);
-    vals[a] = x;
-}
-
 // Packed max-scan: high word = start of the old group, low = start of the new group.
 struct LoadRoundHead {
     const uint64_t *k;
@@ -184,39 +173,6 @@ struct LoadRoundHead {
         return (gnew ? ((uint64_t)a << 32) : 0ull) | (knew ? (uint64_t)a : 0ull);
     }
 };
-template <typename Rem>
-struct StoreRound {
-    ActiveTest<Rem> t;
-    int lb;
-    uint32_t *isa;
-    uint32_t *head;
-    uint32_t *sa;
-    __device__ __forceinline__ void operator()(size_t a, uint64_t inc, uint64_t) const
-    {
-        const uint32_t g = (uint32_t)(t.k[a] >> lb);
-        const uint32_t ag = (uint32_t)(inc >> 32), s2 = (uint32_t)inc;
-        const uint32_t nh = g + (s2 - ag);
-        const uint32_t x = t.vals[a];
-        isa[x] = nh;
-        head[a] = nh;
-        if (t.done(a)) sa[g + ((uint32_t)a - ag)] = x;
-    }
-};
-template <typename Rem>
-struct StoreActiveR {
-    ActiveTest<Rem> a;
-    const uint32_t *head;
-    uint32_t *act_x;
-    uint32_t *act_g;
-    __device__ __forceinline__ void operator()(size_t t, uint32_t pre, uint32_t v) const
-    {
-        if (v) {
-            act_x[pre] = a.vals[t];
-            act_g[pre] = head[t];
-        }
-    }
-};
-
 // ---------------------------------------------------------------------
 // Segmented round for small groups.  After the first rounds almost every
 // group is small (a repetitive text's copies of one position), so a CTA
