@@ -46,7 +46,6 @@ import importlib
 import json
 import os
 import statistics
-import shutil
 import subprocess
 import sys
 import time
@@ -198,14 +197,6 @@ def _sa_is_child(queue):
     L = oracle.sa_bwt(text)
     dt = time.perf_counter() - t0
     queue.put({"seconds": dt, "n": len(text), "blake2b": hashlib.blake2b(L.tobytes(), digest_size=16).hexdigest()})
-
-
-def _config3_child(path):
-    """Spawned process: writes the 256 MiB versioned Markov text (slow to generate) to `path`."""
-    sys.path.insert(0, ROOT)
-    wl = importlib.import_module(PKG + ".workloads")
-    wl.config3_text().tofile(path + ".part")
-    os.replace(path + ".part", path)
 
 
 def reference_programs(variants):
@@ -439,18 +430,17 @@ def measure_text(args, pkg, text, W, P, small, peak, peak_kind, label):
 
 def run_gpu(args):
     import multiprocessing as mp
-    import tempfile
 
     import numpy as np
 
     ws, rank, local = dist_env()
-    # CPU helpers run in spawned processes (never forked after CUDA is up), and
-    # only once the headline and its end-to-end copies are measured: the
-    # 256 MiB Markov text (slow to generate) during the later sections, the
-    # SA-IS baseline after every GPU measurement
+    # Nothing runs beside the GPU measurements on the host: the 256 MiB Markov
+    # text is generated right before its own section, and the SA-IS baseline
+    # runs in a spawned process (never forked after CUDA is up) after every GPU
+    # measurement.  Host-side work in parallel slowed the end-to-end copies and
+    # the serving latencies.
     ctx = mp.get_context("spawn")
-    sa_queue = sa_proc = c3_proc = None
-    c3_path = None
+    sa_queue = sa_proc = None
 
     import torch
     if ws > 1:
@@ -584,10 +574,6 @@ def run_gpu(args):
     del dev_text, dev_out, host_text, host_out
     st.close()
     torch.cuda.empty_cache()
-    if "config3" in args.sections:
-        c3_path = os.path.join(tempfile.mkdtemp(prefix="gbwt_cfg3_"), "config3.bin")
-        c3_proc = ctx.Process(target=_config3_child, args=(c3_path,), daemon=True)
-        c3_proc.start()
 
     # latency first, before the long sections and while the host is quiet
     if "serving" in args.sections:
@@ -610,16 +596,14 @@ def run_gpu(args):
     if "batched" in args.sections:
         line["batched"] = measure_batched(args, pkg, wl, stream)
         log(f"[rank 0] batched: {line['batched']['value']} MB/s")
-    if c3_proc is not None:
-        c3_proc.join(timeout=600)
-        if os.path.exists(c3_path):
-            t3 = np.fromfile(c3_path, dtype=np.uint8)
-            shutil.rmtree(os.path.dirname(c3_path), ignore_errors=True)
-            res, _ = measure_text(args, pkg, t3, 5, 23, False, peak, peak_kind, CONFIG3_WORKLOAD)
-            line["config3"] = res
-            log(f"[rank 0] config 3: {res['value']} MB/s")
-        else:
-            line["config3"] = {"unavailable": "the 256 MiB text was not generated in time"}
+    if "config3" in args.sections:
+        t0 = time.time()
+        t3 = wl.config3_text()
+        log(f"[rank 0] config 3 text generated ({time.time() - t0:.1f}s)")
+        res, _ = measure_text(args, pkg, t3, 5, 23, False, peak, peak_kind, CONFIG3_WORKLOAD)
+        line["config3"] = res
+        log(f"[rank 0] config 3: {res['value']} MB/s")
+        del t3
     if "cpu" in args.sections:
         sa_queue = ctx.Queue()
         sa_proc = ctx.Process(target=_sa_is_child, args=(sa_queue,), daemon=True)
