@@ -11,8 +11,9 @@
 // Here S comes out of the dictionary suffix order directly: equal suffixes
 // are one group of the prefix-doubling result.  For every group we add the
 // occurrence counts of its phrases (block length) and check whether all
-// preceding bytes agree (run).  Runs are written tile by tile with 16-byte
-// stores.  For mixed groups, every phrase occurrence -- visited in parse
+// preceding bytes agree (run).  Runs are written one group per thread with
+// 16-byte stores (long blocks one CTA each).  For mixed groups, every phrase
+// occurrence -- visited in parse
 // suffix-array order, which is exactly the "rank of the next parse suffix"
 // order the reference sorts by -- emits one (group, byte) element per mixed
 // suffix of its phrase; one stable radix sort by group then places every
