@@ -7,10 +7,12 @@
 //   or when T[s..s+W-1] == T[0..W-1]; window 0 never triggers.
 //   D lists the triggering windows' last positions, then n+W-1.
 //
-// GB300 layout: a CTA owns 4096 window starts; the 4096+W-1 bytes it needs
-// are staged in shared memory with 16-byte loads; every thread pulls its 16
-// windows (+ W-1 halo) into registers with 16-byte shared loads and rolls
-// the hash mod P (h(s+1) = 2h(s) - T[s]*2^W + T[s+W]).  The first-word test
+// GB300 layout: a tile is 4096 window starts; the 4096+W-1 bytes it needs
+// are staged in shared memory with 16-byte loads (a CTA loads several tiles
+// before it uses any); every thread pulls its 16 windows (+ W-1 halo) into
+// registers with 16-byte shared loads and rolls the hash mod P
+// (h(s+1) = 2h(s) - T[s]*2^W + T[s+W]); for W=5, P=16 it hashes four
+// windows at once with packed byte arithmetic instead.  The first-word test
 // rolls an exact packed register for W <= 8 and a 64-bit polynomial
 // fingerprint (verified byte by byte on a hit) for longer windows.  Trigger
 // positions are compacted with popc + a CTA scan; the count pass also

@@ -18,9 +18,14 @@
 // their common string ends within h symbols.  Every group is uniform in
 // whether its strings end within h symbols: the initial keys encode it
 // (dictionary: an explicit bit; parse: the unique last phrase), and a round
-// keyed on isa[x+h] inherits it from the groups of x+h.  Keys are (group, isa[x+h]+1)
-// sorted with the project's stable LSD radix sort; group starts and new heads
-// come from one component-wise max-scan.
+// keyed on isa[x+h] inherits it from the groups of x+h.
+//
+// Round 0 sorts the first keys with the stable LSD radix sort and derives
+// group heads and the active list in one packed scan (the single-text parse
+// instead takes its first ranks straight from the phrase buckets).  Every
+// later round gathers isa[x+h] for the active elements and sorts each group
+// by it inside a CTA (k_seg_sort); the few groups too large for a CTA take
+// one radix sort of their members only.
 #include "prims.cuh"
 #include <stdio.h>
 #include <stdlib.h>
